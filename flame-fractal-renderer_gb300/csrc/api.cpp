@@ -1,0 +1,787 @@
+// C ABI of libffr_gpu.so (include/ffr_gpu.h): context lifetime, device
+// memory admission, launches on a context-owned stream, bounded waits and
+// statistics.  No exception crosses the boundary.
+#include "ffr_gpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "flame.hpp"
+#include "isaac64.cuh"
+#include "launch.h"
+
+using namespace ffr;
+
+namespace {
+
+thread_local std::string g_create_error = "no error";
+
+// Isaac::init with flag = false (src/rng/isaac.hpp:93-131): randmem is the
+// golden-ratio constant mixed 4 times, then mixed once per 8 words.
+void isaac_init_table(unsigned long long out[16])
+{
+    uint64_t a, b, c, d, e, f, g, h;
+    a = b = c = d = e = f = g = h = kIsaacGolden;
+    auto mix = [&]() {
+        a -= e; f ^= h >> 9;  h += a;
+        b -= f; g ^= a << 9;  a += b;
+        c -= g; h ^= b >> 23; b += c;
+        d -= h; a ^= c << 15; c += d;
+        e -= a; b ^= d >> 14; d += e;
+        f -= b; c ^= e << 20; e += f;
+        g -= c; d ^= f >> 17; f += g;
+        h -= d; e ^= g << 14; g += h;
+    };
+    for (int i = 0; i < 4; ++i)
+        mix();
+    for (int i = 0; i < 16; i += 8)
+    {
+        mix();
+        out[i + 0] = a; out[i + 1] = b; out[i + 2] = c; out[i + 3] = d;
+        out[i + 4] = e; out[i + 5] = f; out[i + 6] = g; out[i + 7] = h;
+    }
+}
+
+typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
+typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
+typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
+typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
+
+struct Launchers
+{
+    RenderFn render;
+    OccFn occ;
+    StepFn step;
+    TraceFn trace;
+};
+
+const Launchers kLaunchers[2][3] = {
+    {
+        {launch_render_p0_d1, occupancy_p0_d1, launch_step_p0_d1, launch_trace_p0_d1},
+        {launch_render_p0_d2, occupancy_p0_d2, launch_step_p0_d2, launch_trace_p0_d2},
+        {launch_render_p0_d3, occupancy_p0_d3, launch_step_p0_d3, launch_trace_p0_d3},
+    },
+    {
+        {launch_render_p1_d1, occupancy_p1_d1, launch_step_p1_d1, launch_trace_p1_d1},
+        {launch_render_p1_d2, occupancy_p1_d2, launch_step_p1_d2, launch_trace_p1_d2},
+        {launch_render_p1_d3, occupancy_p1_d3, launch_step_p1_d3, launch_trace_p1_d3},
+    },
+};
+
+} // namespace
+
+struct ffr_ctx
+{
+    ffr_opts opts{};
+    HostFlame flame;
+    std::vector<uint8_t> prog_host;
+    int device = 0;
+    int sm_count = 1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_done = nullptr;
+    unsigned char* d_prog = nullptr;
+    unsigned int* d_counts = nullptr;
+    unsigned int* d_hi = nullptr;
+    double* d_colors = nullptr;
+    DevStats* d_stats = nullptr;
+    unsigned long long* d_scratch = nullptr;   // file staging / reductions
+    size_t scratch_bytes = 0;
+    unsigned int* h_cancel = nullptr;          // mapped pinned flag
+    unsigned int* d_cancel = nullptr;
+    unsigned long long isaac_init[16] = {};
+    // upper bound of any cell's count (decides when high words are needed)
+    unsigned long long count_bound = 0;
+    std::string err = "no error";
+
+    const Launchers& L() const { return kLaunchers[opts.precision][flame.dims - 1]; }
+    size_t buffer_bytes() const
+    {
+        return (size_t)flame.cells * (1 + (size_t)flame.color_dims) * 8;
+    }
+};
+
+namespace {
+
+ffr_status fail(ffr_ctx* c, ffr_status s, const std::string& m)
+{
+    if (c)
+        c->err = m;
+    else
+        g_create_error = m;
+    return s;
+}
+
+ffr_status cuda_fail(ffr_ctx* c, cudaError_t e, const char* where)
+{
+    return fail(c, FFR_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(ctx, call)                                   \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess)                          \
+            return cuda_fail((ctx), e_, #call);         \
+    } while (0)
+
+// wait for the context stream with the context's time limit; on timeout the
+// running kernel is asked to stop through the mapped cancel flag, then
+// waited for once more (its poll interval is 4096 samples).
+ffr_status wait_stream(ffr_ctx* c)
+{
+    CU(c, cudaEventRecord(c->ev_done, c->stream));
+    const uint64_t limit = c->opts.timeout_ms;
+    if (limit == 0)
+    {
+        CU(c, cudaEventSynchronize(c->ev_done));
+        return FFR_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;)
+    {
+        cudaError_t q = cudaEventQuery(c->ev_done);
+        if (q == cudaSuccess)
+            return FFR_OK;
+        if (q != cudaErrorNotReady)
+            return cuda_fail(c, q, "cudaEventQuery");
+        const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+            std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)ms >= limit)
+            break;
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    *(volatile unsigned int*)c->h_cancel = 1u;
+    const auto t1 = std::chrono::steady_clock::now();
+    for (;;)
+    {
+        cudaError_t q = cudaEventQuery(c->ev_done);
+        if (q == cudaSuccess)
+            break;
+        if (q != cudaErrorNotReady)
+            return cuda_fail(c, q, "cudaEventQuery");
+        const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+            std::chrono::steady_clock::now() - t1).count();
+        if ((uint64_t)ms >= std::max<uint64_t>(limit, 1000))
+            return fail(c, FFR_ERR_TIMEOUT, "device work did not stop after cancel");
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    *(volatile unsigned int*)c->h_cancel = 0u;
+    return fail(c, FFR_ERR_TIMEOUT, "render exceeded timeout_ms ("
+        + std::to_string(limit) + " ms) and was cancelled");
+}
+
+ffr_status ensure_scratch(ffr_ctx* c, size_t bytes)
+{
+    if (c->scratch_bytes >= bytes)
+        return FFR_OK;
+    if (c->d_scratch)
+        cudaFree(c->d_scratch);
+    c->d_scratch = nullptr;
+    c->scratch_bytes = 0;
+    size_t fr = 0, tot = 0;
+    CU(c, cudaMemGetInfo(&fr, &tot));
+    if (bytes + (64u << 20) > fr)
+        return fail(c, FFR_ERR_OOM, "not enough free device memory for a "
+            + std::to_string(bytes) + "-byte staging buffer");
+    CU(c, cudaMalloc(&c->d_scratch, bytes));
+    c->scratch_bytes = bytes;
+    return FFR_OK;
+}
+
+ffr_status ensure_hi(ffr_ctx* c)
+{
+    if (c->d_hi)
+        return FFR_OK;
+    CU(c, cudaMalloc(&c->d_hi, c->flame.cells * sizeof(unsigned int)));
+    CU(c, cudaMemsetAsync(c->d_hi, 0, c->flame.cells * sizeof(unsigned int), c->stream));
+    return FFR_OK;
+}
+
+void destroy(ffr_ctx* c)
+{
+    if (!c)
+        return;
+    cudaSetDevice(c->device);
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_prog);
+    cudaFree(c->d_counts);
+    cudaFree(c->d_hi);
+    cudaFree(c->d_colors);
+    cudaFree(c->d_stats);
+    cudaFree(c->d_scratch);
+    if (c->h_cancel)
+        cudaFreeHost(c->h_cancel);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
+    if (c->stream)
+        cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+ffr_status plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* L, int* grid)
+{
+    int bps = 0, block = 0;
+    size_t smem = 0;
+    CU(c, c->L().occ(c->flame.color_dims > 0, c->d_hi != nullptr, &bps, &block,
+                     (unsigned int)c->prog_host.size(), (int)c->flame.xforms.size(), &smem));
+    if (bps < 1)
+        return fail(c, FFR_ERR_ARG, "render kernel does not fit on an SM "
+            "(program " + std::to_string(c->prog_host.size()) + " bytes)");
+    const uint64_t resident = (uint64_t)c->sm_count * bps * block;
+    uint64_t S = c->opts.streams ? c->opts.streams : resident;
+    uint64_t len = c->opts.traj_len;
+    if (len == 0)
+        len = samples ? std::max<uint64_t>(1, (samples + S - 1) / S) : 1;
+    const uint64_t ntraj = samples ? (samples + len - 1) / len : 0;
+    const uint64_t active = std::min<uint64_t>(S, ntraj);
+    uint64_t blocks = (active + block - 1) / block;
+    blocks = std::min<uint64_t>(blocks, (uint64_t)c->sm_count * bps);
+    if (blocks < 1)
+        blocks = 1;
+    // per-thread xform counters are u32: bound one thread's samples
+    const uint64_t threads = blocks * block;
+    const uint64_t streams_per_thread = (active + threads - 1) / threads;
+    const uint64_t traj_per_stream = S ? (ntraj + S - 1) / S : 0;
+    const long double per_thread = (long double)streams_per_thread * traj_per_stream * len;
+    if (per_thread >= 4294967296.0L)
+        return fail(c, FFR_ERR_ARG, "too many samples per GPU thread (raise streams)");
+    *streams = S;
+    *L = len;
+    *grid = (int)blocks;
+    return FFR_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void ffr_default_opts(ffr_opts* o)
+{
+    if (!o)
+        return;
+    std::memset(o, 0, sizeof *o);
+    o->abi_version = FFR_ABI_VERSION;
+    o->device = 0;
+    o->precision = FFR_FP64;
+    o->settle = 53;
+    o->streams = 0;
+    o->traj_len = 0;
+    o->timeout_ms = 0;
+}
+
+ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ctx** out)
+{
+    if (!out)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_create: out is NULL");
+    *out = nullptr;
+    if (!json)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_create: json is NULL");
+    ffr_opts o;
+    if (opts)
+        o = *opts;
+    else
+        ffr_default_opts(&o);
+    if (o.abi_version != FFR_ABI_VERSION)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_create: ABI version mismatch");
+    if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown precision");
+    ffr_ctx* c = new (std::nothrow) ffr_ctx;
+    if (!c)
+        return fail(nullptr, FFR_ERR_OOM, "ffr_create: out of host memory");
+    c->opts = o;
+    try
+    {
+        c->flame = parse_flame(std::string(json, len));
+        c->prog_host = o.precision == FFR_FP64 ? build_program<double>(c->flame)
+                                               : build_program<float>(c->flame);
+    }
+    catch (const FlameError& e)
+    {
+        delete c;
+        return fail(nullptr, FFR_ERR_PARSE, e.what());
+    }
+    catch (const std::exception& e)
+    {
+        delete c;
+        return fail(nullptr, FFR_ERR_PARSE, e.what());
+    }
+    if (c->flame.xforms.size() > (size_t)kMaxXformIds)
+    {
+        delete c;
+        return fail(nullptr, FFR_ERR_ARG, "too many xforms");
+    }
+    c->device = o.device;
+    auto cfail = [&](cudaError_t e, const char* what) {
+        std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+        destroy(c);
+        return fail(nullptr, FFR_ERR_CUDA, m);
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(c->device)) != cudaSuccess)
+        return cfail(e, "cudaSetDevice");
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cfail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess
+            || (e = cudaEventCreate(&c->ev1)) != cudaSuccess
+            || (e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming)) != cudaSuccess)
+        return cfail(e, "cudaEventCreate");
+    if ((e = cudaHostAlloc(&c->h_cancel, sizeof(unsigned int), cudaHostAllocMapped)) != cudaSuccess)
+        return cfail(e, "cudaHostAlloc");
+    *c->h_cancel = 0;
+    if ((e = cudaHostGetDevicePointer(&c->d_cancel, c->h_cancel, 0)) != cudaSuccess)
+        return cfail(e, "cudaHostGetDevicePointer");
+    // admission by free device memory
+    const size_t need = c->flame.cells * sizeof(unsigned int)
+        + c->flame.cells * (size_t)c->flame.color_dims * sizeof(double)
+        + sizeof(DevStats) + c->prog_host.size();
+    size_t fr = 0, tot = 0;
+    if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess)
+        return cfail(e, "cudaMemGetInfo");
+    if (need + (256u << 20) > fr)
+    {
+        destroy(c);
+        return fail(nullptr, FFR_ERR_OOM, "buffer needs " + std::to_string(need)
+            + " bytes of device memory, " + std::to_string(fr) + " free");
+    }
+    if ((e = cudaMalloc(&c->d_prog, c->prog_host.size())) != cudaSuccess)
+        return cfail(e, "cudaMalloc(program)");
+    if ((e = cudaMalloc(&c->d_counts, c->flame.cells * sizeof(unsigned int))) != cudaSuccess)
+        return cfail(e, "cudaMalloc(counts)");
+    if (c->flame.color_dims
+            && (e = cudaMalloc(&c->d_colors, c->flame.cells * c->flame.color_dims * sizeof(double))) != cudaSuccess)
+        return cfail(e, "cudaMalloc(colors)");
+    if ((e = cudaMalloc(&c->d_stats, sizeof(DevStats))) != cudaSuccess)
+        return cfail(e, "cudaMalloc(stats)");
+    if ((e = cudaMemcpyAsync(c->d_prog, c->prog_host.data(), c->prog_host.size(),
+                             cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
+        return cfail(e, "cudaMemcpy(program)");
+    if ((e = cudaMemsetAsync(c->d_counts, 0, c->flame.cells * sizeof(unsigned int), c->stream)) != cudaSuccess)
+        return cfail(e, "cudaMemset(counts)");
+    if (c->d_colors
+            && (e = cudaMemsetAsync(c->d_colors, 0, c->flame.cells * c->flame.color_dims * sizeof(double), c->stream)) != cudaSuccess)
+        return cfail(e, "cudaMemset(colors)");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+        return cfail(e, "cudaStreamSynchronize");
+    isaac_init_table(c->isaac_init);
+    *out = c;
+    return FFR_OK;
+}
+
+void ffr_destroy(ffr_ctx* c)
+{
+    destroy(c);
+}
+
+const char* ffr_last_error(const ffr_ctx* c)
+{
+    return c ? c->err.c_str() : g_create_error.c_str();
+}
+
+ffr_status ffr_info(const ffr_ctx* c, uint32_t* dims, uint64_t* cells,
+                    uint32_t* color_dims, size_t* buffer_bytes)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (dims) *dims = (uint32_t)c->flame.dims;
+    if (cells) *cells = c->flame.cells;
+    if (color_dims) *color_dims = (uint32_t)c->flame.color_dims;
+    if (buffer_bytes) *buffer_bytes = c->buffer_bytes();
+    return FFR_OK;
+}
+
+ffr_status ffr_size(const ffr_ctx* c, uint64_t* size)
+{
+    if (!c || !size)
+        return FFR_ERR_ARG;
+    for (int i = 0; i < c->flame.dims; ++i)
+        size[i] = c->flame.size[i];
+    return FFR_OK;
+}
+
+const char* ffr_flame_json(const ffr_ctx* c)
+{
+    return c ? c->flame.echo.c_str() : "";
+}
+
+static ffr_status import_file(ffr_ctx* c, const void* cells, size_t bytes, int overwrite)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (!cells && bytes)
+        return fail(c, FFR_ERR_ARG, "buffer pointer is NULL");
+    const size_t need = c->buffer_bytes();
+    if (bytes < need)
+        return fail(c, FFR_ERR_IO, "error reading file: buffer has " + std::to_string(bytes)
+            + " bytes, flame needs " + std::to_string(need));
+    CU(c, cudaSetDevice(c->device));
+    ffr_status s = ensure_scratch(c, need + 64);
+    if (s != FFR_OK)
+        return s;
+    unsigned long long* dmax = c->d_scratch + need / 8;
+    CU(c, cudaMemcpyAsync(c->d_scratch, cells, need, cudaMemcpyHostToDevice, c->stream));
+    // counts reaching 2^32 need the high-word plane
+    CU(c, cudaMemsetAsync(dmax, 0, 8, c->stream));
+    CU(c, launch_file_max(c->d_scratch, c->flame.cells, c->flame.color_dims, dmax, c->stream));
+    unsigned long long file_max = 0;
+    CU(c, cudaMemcpyAsync(&file_max, dmax, 8, cudaMemcpyDeviceToHost, c->stream));
+    CU(c, cudaStreamSynchronize(c->stream));
+    const long double bound = overwrite ? (long double)file_max
+                                        : (long double)c->count_bound + file_max;
+    if (bound >= 4294967295.0L)
+    {
+        s = ensure_hi(c);
+        if (s != FFR_OK)
+            return s;
+    }
+    CU(c, launch_accumulate(c->d_scratch, c->flame.cells, c->flame.color_dims, c->d_counts,
+                            c->d_hi, c->d_colors, overwrite, c->stream));
+    s = wait_stream(c);
+    if (s != FFR_OK)
+        return s;
+    // tighten the bound from the actual maximum
+    uint64_t sum = 0, mn = 0, mx = 0;
+    s = ffr_histogram(c, &sum, &mn, &mx);
+    if (s != FFR_OK)
+        return s;
+    c->count_bound = mx;
+    return FFR_OK;
+}
+
+ffr_status ffr_add_buffer(ffr_ctx* c, const void* cells, size_t bytes)
+{
+    return import_file(c, cells, bytes, 0);
+}
+
+ffr_status ffr_load_buffer(ffr_ctx* c, const void* cells, size_t bytes)
+{
+    return import_file(c, cells, bytes, 1);
+}
+
+ffr_status ffr_plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* traj_len)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    CU(c, cudaSetDevice(c->device));
+    uint64_t S = 0, L = 0;
+    int grid = 0;
+    ffr_status s = plan(c, samples, &S, &L, &grid);
+    if (s != FFR_OK)
+        return s;
+    if (streams) *streams = S;
+    if (traj_len) *traj_len = L;
+    return FFR_OK;
+}
+
+ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_limit,
+                      ffr_stats* st)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (st)
+    {
+        std::memset(st, 0, sizeof *st);
+        for (int i = 0; i < FFR_MAX_DIMS; ++i)
+        {
+            st->ext_lo[i] = INFINITY;
+            st->ext_hi[i] = -INFINITY;
+        }
+        st->xform_ids = c->flame.xform_ids;
+        st->settle = c->opts.settle;
+    }
+    if (samples == 0)
+        return FFR_OK;      // render(0) returns true (buffer_renderer.hpp:276-277)
+    CU(c, cudaSetDevice(c->device));
+    if (c->count_bound + samples >= 0xFFFFFFFFULL)
+    {
+        ffr_status s = ensure_hi(c);
+        if (s != FFR_OK)
+            return s;
+    }
+    uint64_t S = 0, L = 0;
+    int grid = 0;
+    ffr_status s = plan(c, samples, &S, &L, &grid);
+    if (s != FFR_OK)
+        return s;
+    // reset device stats: zero, then +inf / -inf extreme keys
+    DevStats head;
+    std::memset(&head, 0, offsetof(DevStats, xf_dist));
+    for (int i = 0; i < kMaxDims; ++i)
+    {
+        head.ext_lo[i] = order_key(INFINITY);
+        head.ext_hi[i] = order_key(-INFINITY);
+    }
+    CU(c, cudaMemcpyAsync(c->d_stats, &head, offsetof(DevStats, xf_dist),
+                          cudaMemcpyHostToDevice, c->stream));
+    CU(c, cudaMemsetAsync(c->d_stats->xf_dist, 0,
+                          sizeof(unsigned long long) * c->flame.xforms.size(), c->stream));
+    RenderArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.prog = c->d_prog;
+    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.nxf = (int)c->flame.xforms.size();
+    a.color_dims = c->flame.color_dims;
+    a.spill = c->d_hi != nullptr;
+    a.seed = seed;
+    a.streams = S;
+    a.samples = samples;
+    a.traj_len = L;
+    a.settle = c->opts.settle;
+    a.bad_limit = bad_limit;
+    a.counts = c->d_counts;
+    a.hi = c->d_hi;
+    a.colors = c->d_colors;
+    a.stats = c->d_stats;
+    a.cancel = c->d_cancel;
+    std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+    *c->h_cancel = 0u;
+    CU(c, cudaEventRecord(c->ev0, c->stream));
+    CU(c, c->L().render(a, grid, c->stream));
+    CU(c, cudaEventRecord(c->ev1, c->stream));
+    s = wait_stream(c);
+    c->count_bound += samples;
+    if (s != FFR_OK)
+        return s;
+    DevStats* hs = new (std::nothrow) DevStats;
+    if (!hs)
+        return fail(c, FFR_ERR_OOM, "out of host memory");
+    CU(c, cudaMemcpy(hs, c->d_stats, offsetof(DevStats, xf_dist), cudaMemcpyDeviceToHost));
+    const size_t nxf = c->flame.xforms.size();
+    CU(c, cudaMemcpy(hs->xf_dist, c->d_stats->xf_dist, sizeof(unsigned long long) * nxf,
+                     cudaMemcpyDeviceToHost));
+    const unsigned long long nrec = std::min<unsigned long long>(hs->bad_claim, kMaxBadRecords);
+    if (nrec)
+    {
+        CU(c, cudaMemcpy(hs->bad_xf, c->d_stats->bad_xf, sizeof(unsigned long long) * nrec,
+                         cudaMemcpyDeviceToHost));
+        CU(c, cudaMemcpy(hs->bad_pts, c->d_stats->bad_pts, sizeof(double) * kMaxDims * nrec,
+                         cudaMemcpyDeviceToHost));
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    const bool failed = hs->stop != 0;
+    if (st)
+    {
+        st->samples_iterated = hs->s_iter;
+        st->samples_plotted = hs->s_plot;
+        st->bad_values = hs->bad_total;
+        st->dropped = hs->dropped;
+        for (int i = 0; i < c->flame.dims; ++i)
+        {
+            st->ext_lo[i] = key_to_double(hs->ext_lo[i]);
+            st->ext_hi[i] = key_to_double(hs->ext_hi[i]);
+        }
+        for (size_t k = 0; k < nxf; ++k)
+        {
+            const uint64_t id = c->flame.xforms[k].id;
+            if (id < FFR_MAX_XFORM_IDS)
+                st->xf_dist[id] += hs->xf_dist[k];
+        }
+        st->bad_recorded = nrec;
+        for (unsigned long long k = 0; k < nrec; ++k)
+        {
+            st->bad_xf[k] = hs->bad_xf[k];
+            for (int i = 0; i < c->flame.dims; ++i)
+                st->bad_pts[k][i] = hs->bad_pts[k][i];
+        }
+        st->streams = S;
+        st->traj_len = L;
+        st->kernel_ms = ms;
+    }
+    const bool cancelled = hs->cancelled != 0;
+    delete hs;
+    if (cancelled)
+        return fail(c, FFR_ERR_TIMEOUT, "render cancelled");
+    if (failed)
+        return fail(c, FFR_BAD_VALUES, "render failure (flame may not be sufficiently contractive)");
+    return FFR_OK;
+}
+
+ffr_status ffr_read_buffer(ffr_ctx* c, void* cells, size_t bytes)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    const size_t need = c->buffer_bytes();
+    if (!cells || bytes < need)
+        return fail(c, FFR_ERR_IO, "error writing output: destination too small");
+    CU(c, cudaSetDevice(c->device));
+    ffr_status s = ensure_scratch(c, need + 64);
+    if (s != FFR_OK)
+        return s;
+    CU(c, launch_export(c->d_scratch, c->flame.cells, c->flame.color_dims, c->d_counts,
+                        c->d_hi, c->d_colors, c->stream));
+    CU(c, cudaMemcpyAsync(cells, c->d_scratch, need, cudaMemcpyDeviceToHost, c->stream));
+    return wait_stream(c);
+}
+
+ffr_status ffr_histogram(ffr_ctx* c, uint64_t* sum, uint64_t* mn, uint64_t* mx)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    CU(c, cudaSetDevice(c->device));
+    ffr_status s = ensure_scratch(c, 64);
+    if (s != FFR_OK)
+        return s;
+    unsigned long long init[3] = {0ull, ~0ull, 0ull}, out[3];
+    unsigned long long* d = c->d_scratch + (c->scratch_bytes / 8 - 4);
+    CU(c, cudaMemcpyAsync(d, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
+    CU(c, launch_hist_reduce(c->d_counts, c->d_hi, c->flame.cells, d, c->stream));
+    CU(c, cudaMemcpyAsync(out, d, sizeof out, cudaMemcpyDeviceToHost, c->stream));
+    s = wait_stream(c);
+    if (s != FFR_OK)
+        return s;
+    if (sum) *sum = out[0];
+    if (mn) *mn = out[1];
+    if (mx) *mx = out[2];
+    return FFR_OK;
+}
+
+ffr_status ffr_clear(ffr_ctx* c)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    CU(c, cudaSetDevice(c->device));
+    CU(c, cudaMemsetAsync(c->d_counts, 0, c->flame.cells * sizeof(unsigned int), c->stream));
+    if (c->d_hi)
+        CU(c, cudaMemsetAsync(c->d_hi, 0, c->flame.cells * sizeof(unsigned int), c->stream));
+    if (c->d_colors)
+        CU(c, cudaMemsetAsync(c->d_colors, 0,
+                              c->flame.cells * c->flame.color_dims * sizeof(double), c->stream));
+    c->count_bound = 0;
+    return wait_stream(c);
+}
+
+ffr_status ffr_isaac_words(int device, uint64_t key, uint64_t n, uint64_t* out)
+{
+    if (!out && n)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_isaac_words: out is NULL");
+    if (n == 0)
+        return FFR_OK;
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "cudaSetDevice");
+    unsigned long long init[16];
+    isaac_init_table(init);
+    unsigned long long* d = nullptr;
+    if ((e = cudaMalloc(&d, n * 8)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "cudaMalloc");
+    e = launch_isaac_words(key, n, d, init, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, d, n * 8, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return cuda_fail(nullptr, e, "ffr_isaac_words");
+    return FFR_OK;
+}
+
+ffr_status ffr_measure_atomic_rate(int device, uint64_t cells, uint64_t ops,
+                                   double* ops_per_s)
+{
+    if (!ops_per_s || cells == 0 || cells > 0xFFFFFFFFull || ops == 0)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_measure_atomic_rate: bad arguments");
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "cudaSetDevice");
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int block = 256, grid = sms * 8;
+    const uint64_t threads = (uint64_t)grid * block;
+    const unsigned int iters = (unsigned int)std::max<uint64_t>(1, ops / threads);
+    unsigned int* buf = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    float ms = 0.f;
+    if ((e = cudaMalloc(&buf, cells * 4)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "cudaMalloc");
+    e = cudaMemset(buf, 0, cells * 4);
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    // one warm-up launch, then the timed one
+    if (e == cudaSuccess) e = launch_atomic_rate(buf, (unsigned int)cells, iters, grid, block, 1u, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(a, 0);
+    if (e == cudaSuccess) e = launch_atomic_rate(buf, (unsigned int)cells, iters, grid, block, 2u, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(b, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(buf);
+    if (e != cudaSuccess)
+        return cuda_fail(nullptr, e, "ffr_measure_atomic_rate");
+    *ops_per_s = (double)threads * iters / (ms * 1e-3);
+    return FFR_OK;
+}
+
+ffr_status ffr_step(ffr_ctx* c, int xf_index, uint64_t key, uint64_t npts,
+                    const double* in, double* out)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (xf_index < -1 || xf_index >= (int)c->flame.xforms.size()
+            || (xf_index == -1 && !c->flame.has_final))
+        return fail(c, FFR_ERR_ARG, "ffr_step: no such xform");
+    if (npts == 0)
+        return FFR_OK;
+    CU(c, cudaSetDevice(c->device));
+    const size_t bytes = npts * (size_t)c->flame.dims * sizeof(double);
+    ffr_status s = ensure_scratch(c, 2 * bytes + 64);
+    if (s != FFR_OK)
+        return s;
+    double* din = reinterpret_cast<double*>(c->d_scratch);
+    double* dout = din + npts * c->flame.dims;
+    CU(c, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, c->stream));
+    StepArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.prog = c->d_prog;
+    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.xf_index = xf_index;
+    a.key = key;
+    a.npts = npts;
+    a.in = din;
+    a.out = dout;
+    std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+    CU(c, c->L().step(a, c->stream));
+    CU(c, cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return wait_stream(c);
+}
+
+ffr_status ffr_trace(ffr_ctx* c, uint64_t key, uint64_t settle, uint64_t n,
+                     int32_t* ids, double* pts)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (n == 0)
+        return FFR_OK;
+    CU(c, cudaSetDevice(c->device));
+    const size_t pbytes = n * (size_t)c->flame.dims * sizeof(double);
+    const size_t ibytes = (n * sizeof(int32_t) + 15) & ~(size_t)15;
+    ffr_status s = ensure_scratch(c, pbytes + ibytes + 64);
+    if (s != FFR_OK)
+        return s;
+    double* dp = reinterpret_cast<double*>(c->d_scratch);
+    int* di = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(c->d_scratch) + pbytes);
+    TraceArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.prog = c->d_prog;
+    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.key = key;
+    a.settle = settle;
+    a.n = n;
+    a.ids = di;
+    a.pts = dp;
+    std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+    CU(c, c->L().trace(a, c->stream));
+    CU(c, cudaMemcpyAsync(pts, dp, pbytes, cudaMemcpyDeviceToHost, c->stream));
+    CU(c, cudaMemcpyAsync(ids, di, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    return wait_stream(c);
+}
+
+} // extern "C"

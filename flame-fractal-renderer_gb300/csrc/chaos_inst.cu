@@ -1,0 +1,101 @@
+// Instantiates the chaos kernels for one (precision, dims) pair; compiled
+// once per pair with -DFFR_P=<0|1> -DFFR_D=<1|2|3>.  The FP64 objects are
+// built with --fmad=false so no multiply-add is contracted: the reference
+// (and the oracle) round every product and sum separately.
+#include "chaos_kernel.cuh"
+
+#if !defined(FFR_P) || !defined(FFR_D)
+#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3>"
+#endif
+
+#define FFR_CAT2(a, b, c, d) a##_p##b##_d##c##d
+#define FFR_CAT(a, b, c) FFR_CAT2(a, b, c, )
+#define FFR_NAME(a) FFR_CAT(a, FFR_P, FFR_D)
+
+namespace ffr {
+
+#if FFR_P == 0
+using Real = double;
+#else
+using Real = float;
+#endif
+
+constexpr int kBlock = 128;
+
+template <bool C, bool S>
+static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf);
+    auto k = chaos_kernel<FFR_D, Real, C, S, kBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, kBlock, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool C, bool S>
+static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, size_t* smem_out)
+{
+    const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf);
+    auto k = chaos_kernel<FFR_D, Real, C, S, kBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    *smem_out = smem;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kBlock, smem);
+}
+
+cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    const bool color = a.color_dims > 0;
+    if (color)
+        return a.spill ? launch_one<true, true>(a, grid, st)
+                       : launch_one<true, false>(a, grid, st);
+    return a.spill ? launch_one<false, true>(a, grid, st)
+                   : launch_one<false, false>(a, grid, st);
+}
+
+cudaError_t FFR_NAME(occupancy)(int color, int spill, int* blocks_per_sm, int* block,
+                                unsigned int prog_bytes, int nxf, size_t* smem)
+{
+    *block = kBlock;
+    if (color)
+        return spill ? occ_one<true, true>(blocks_per_sm, prog_bytes, nxf, smem)
+                     : occ_one<true, false>(blocks_per_sm, prog_bytes, nxf, smem);
+    return spill ? occ_one<false, true>(blocks_per_sm, prog_bytes, nxf, smem)
+                 : occ_one<false, false>(blocks_per_sm, prog_bytes, nxf, smem);
+}
+
+cudaError_t FFR_NAME(launch_step)(const StepArgs& a, cudaStream_t st)
+{
+    if (a.npts == 0)
+        return cudaSuccess;
+    const size_t smem = align16u(a.prog_bytes) + 2 * 16 * 128 * sizeof(uint64_t);
+    auto k = step_kernel<FFR_D, Real>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    unsigned long long blocks = (a.npts + 127) / 128;
+    if (blocks > 65535)
+        blocks = 65535;
+    k<<<(unsigned int)blocks, 128, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t FFR_NAME(launch_trace)(const TraceArgs& a, cudaStream_t st)
+{
+    const size_t smem = align16u(a.prog_bytes) + 2 * 16 * sizeof(uint64_t);
+    auto k = trace_kernel<FFR_D, Real>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k<<<1, 1, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace ffr

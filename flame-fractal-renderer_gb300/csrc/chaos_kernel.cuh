@@ -1,0 +1,520 @@
+// Chaos-game kernels: one GPU thread = one ISAAC stream running its
+// trajectories in order.  Replaces, per stream, the reference's
+//   BufferRenderer::_render_batch   src/renderers/buffer_renderer.hpp:151-250
+//   RenderIterator::_init/iterate   src/renderers/render_iterator.hpp:52-139
+//   Flame::getRandomXForm           src/types/flame.hpp:212-219
+//   XForm::applyIteration           src/types/xform.hpp:211-227
+//   Affine::apply_to                src/types/affine.hpp:104-110
+// and, across the grid, BufferRenderer::render's thread pool
+// (buffer_renderer.hpp:269-338): trajectory j of the job runs on stream
+// j mod streams, stream s seeded with setSeed(seed + fmix64(s)).
+//
+// Shared memory per CTA: the flame program (copied once), the ISAAC state
+// [16][BLOCK] x2, and per-thread xform counters [nxf][BLOCK] (u32) when
+// nxf <= kLocalXfCounters, else one u64 counter per xform for the CTA.
+// Binning: one relaxed atomic add per in-bounds sample into the u32 count
+// buffer (fire-and-forget RED unless counts can pass 2^32, in which case the
+// returned old value carries into the u32 high-word buffer).
+#pragma once
+
+#include <cstdint>
+
+#include "flame_program.h"
+#include "isaac64.cuh"
+#include "launch.h"
+#include "variations.cuh"
+
+namespace ffr {
+
+constexpr int kLocalXfCounters = 16;
+constexpr int kStopPollMask = 4095;     // poll stop/cancel every 4096 samples
+
+__host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
+
+template <int BLOCK>
+__host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf)
+{
+    size_t s = align16u(prog_bytes);
+    s += 2 * 16 * (size_t)BLOCK * sizeof(uint64_t);
+    if (nxf <= kLocalXfCounters)
+        s += (size_t)nxf * BLOCK * sizeof(uint32_t);
+    else
+        s += (size_t)nxf * sizeof(unsigned long long);
+    return s;
+}
+
+// Program view over the shared-memory copy
+template <typename R>
+struct Prog
+{
+    const ProgHeader<R>* h;
+    const uint64_t* thresh;
+    const XformT<R>* xf;
+    const VarT<R>* var;
+    const R* color;
+
+    __device__ __forceinline__ void bind(const unsigned char* base)
+    {
+        h = reinterpret_cast<const ProgHeader<R>*>(base);
+        thresh = reinterpret_cast<const uint64_t*>(base + h->off_thresh);
+        xf = reinterpret_cast<const XformT<R>*>(base + h->off_xf);
+        var = reinterpret_cast<const VarT<R>*>(base + h->off_var);
+        color = reinterpret_cast<const R*>(base + h->off_color);
+    }
+};
+
+// cooperative 16-byte copy of the program into shared memory
+template <int BLOCK>
+__device__ __forceinline__ void load_program(unsigned char* dst, const unsigned char* src,
+                                             unsigned int bytes)
+{
+    for (unsigned int k = threadIdx.x * 16u; k < bytes; k += BLOCK * 16u)
+        *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
+}
+
+// Affine::apply_to: ret = b; ret[i] += (0 + A[i][0] x[0] + ...)
+template <int D, typename R>
+__device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
+{
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+    {
+        R d = R(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+            d += aff[i * kMaxDims + j] * x[j];
+        out[i] = aff[kMaxDims * kMaxDims + i] + d;
+    }
+}
+
+// XForm::applyIteration (xform.hpp:211-227).  For dims < 3 both affines are
+// always applied (identity when absent), for dims >= 3 only when present.
+template <int D, typename R, typename Rng>
+__device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& x,
+                                            const R* p, R* out, Rng& rng)
+{
+    R t[D], v[D];
+    if (D < 3 || x.has_pre)
+        affine<D>(x.pre, p, t);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            t[i] = p[i];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        v[i] = R(0);
+    const int vb = x.var_begin, ve = x.var_begin + x.var_count;
+    for (int k = vb; k < ve; ++k)
+    {
+        const VarT<R>& var = pg.var[k];
+        R o[D];
+        variation<D, R>(var, t, o, rng);
+        const R w = var.weight;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] += o[i] * w;
+    }
+    if (D < 3 || x.has_post)
+        affine<D>(x.post, v, out);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            out[i] = v[i];
+    }
+}
+
+// Flame::getRandomXForm via exact integer thresholds (flame_program.h)
+template <typename R, typename Rng>
+__device__ __forceinline__ int pick_xform(const Prog<R>& pg, Rng& rng)
+{
+    const uint64_t m = rng.next() >> 11;
+    int i = 0;
+    while (m > pg.thresh[i])
+        ++i;
+    return i;
+}
+
+template <int D, typename R>
+__device__ __forceinline__ bool bad_point(const R* p)
+{
+    bool b = false;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        b |= (RealTraits<R>::fabs_(p[i]) > RealTraits<R>::bad) || (p[i] != p[i]);
+    return b;
+}
+
+template <typename R> __device__ __forceinline__ uint64_t to_index(R x);
+template <> __device__ __forceinline__ uint64_t to_index<double>(double x)
+{
+    return (uint64_t)x;     // size_t conversion truncates (buffer_renderer.hpp:202)
+}
+template <> __device__ __forceinline__ uint64_t to_index<float>(float x)
+{
+    return (uint64_t)x;
+}
+
+template <typename R>
+__device__ __forceinline__ double as_double(R x) { return (double)x; }
+
+template <int D, typename R, bool COLOR, bool SPILL, int BLOCK>
+__device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem)
+{
+    using T = RealTraits<R>;
+    Prog<R> pg;
+    pg.bind(smem);
+    const ProgHeader<R>& h = *pg.h;
+    const int nxf = a.nxf;
+    uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
+    uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + 2 * 16 * BLOCK);
+    unsigned long long* xfc_shared = reinterpret_cast<unsigned long long*>(xfc_local);
+    const bool local_xfc = nxf <= kLocalXfCounters;
+    if (local_xfc)
+    {
+        for (int i = 0; i < nxf; ++i)
+            xfc_local[i * BLOCK + threadIdx.x] = 0u;
+    }
+    else
+    {
+        for (int i = threadIdx.x; i < nxf; i += BLOCK)
+            xfc_shared[i] = 0ull;
+        __syncthreads();
+    }
+
+    DevIsaac<BLOCK> rng;
+    rng.mem = ismem + threadIdx.x;
+    rng.rsl = ismem + 16 * BLOCK + threadIdx.x;
+
+    unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
+    R ext_lo[D], ext_hi[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+    {
+        ext_lo[i] = R(1) / R(0);
+        ext_hi[i] = -R(1) / R(0);
+    }
+    const int r = COLOR ? a.color_dims : 0;
+    R c[COLOR ? kMaxColorDims : 1], cf[COLOR ? kMaxColorDims : 1];
+    (void)c; (void)cf;
+
+    const unsigned long long L = a.traj_len;
+    const unsigned long long ntraj = (a.samples + L - 1) / L;
+    const unsigned long long nstreams = a.streams < ntraj ? a.streams : ntraj;
+    const unsigned long long gstride = (unsigned long long)gridDim.x * BLOCK;
+    bool stop = false;
+    volatile unsigned int* vstop = &a.stats->stop;
+
+    for (unsigned long long s = (unsigned long long)blockIdx.x * BLOCK + threadIdx.x;
+         s < nstreams && !stop; s += gstride)
+    {
+        rng.seed(stream_key(a.seed, s), a.isaac_init);
+        for (unsigned long long tj = s; tj < ntraj && !stop; tj += a.streams)
+        {
+            unsigned long long len = a.samples - tj * L;
+            if (len > L)
+                len = L;
+            // _render_batch entry check (buffer_renderer.hpp:153)
+            if (*vstop)
+            {
+                stop = true;
+                break;
+            }
+            R p[D], pf[D];
+            // RenderIterator::_init (render_iterator.hpp:52-60)
+            auto init = [&]() {
+#pragma unroll
+                for (int i = 0; i < D; ++i)
+                    p[i] = R(2) * T::unit(rng.next()) - R(1);
+                for (unsigned long long k = 0; k < a.settle; ++k)
+                {
+                    const int xi = pick_xform<R>(pg, rng);
+                    R q[D];
+                    apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
+#pragma unroll
+                    for (int i = 0; i < D; ++i)
+                        p[i] = q[i];
+                }
+                if (COLOR)
+                    for (int i = 0; i < r; ++i)
+                        c[i] = T::unit(rng.next());
+            };
+            init();
+            unsigned int poll = 0;
+            for (; len > 0; --len)
+            {
+                const int xi = pick_xform<R>(pg, rng);
+                const XformT<R>& xf = pg.xf[xi];
+                {
+                    R q[D];
+                    apply_xform<D, R>(pg, xf, p, q, rng);
+#pragma unroll
+                    for (int i = 0; i < D; ++i)
+                        p[i] = q[i];
+                }
+                if (COLOR && xf.has_color)
+                {
+                    const R sp = xf.color_speed;
+                    const R* col = pg.color + (size_t)xi * r;
+                    for (int i = 0; i < r; ++i)
+                        c[i] = (R(1) - sp) * c[i] + sp * col[i];
+                }
+                if (h.has_final)
+                {
+                    const XformT<R>& ff = pg.xf[nxf];
+                    apply_xform<D, R>(pg, ff, p, pf, rng);
+                    if (COLOR)
+                    {
+                        if (ff.has_color)
+                        {
+                            const R sp = ff.color_speed;
+                            const R* col = pg.color + (size_t)nxf * r;
+                            for (int i = 0; i < r; ++i)
+                                cf[i] = (R(1) - sp) * c[i] + sp * col[i];
+                        }
+                        else
+                            for (int i = 0; i < r; ++i)
+                                cf[i] = c[i];
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int i = 0; i < D; ++i)
+                        pf[i] = p[i];
+                    if (COLOR)
+                        for (int i = 0; i < r; ++i)
+                            cf[i] = c[i];
+                }
+                ++s_iter;
+                if (local_xfc)
+                    ++xfc_local[xi * BLOCK + threadIdx.x];
+                else
+                    atomicAdd(&xfc_shared[xi], 1ull);
+                // bad value (buffer_renderer.hpp:175-186)
+                if (bad_point<D, R>(p))
+                {
+                    const unsigned long long tot = atomicAdd(&a.stats->bad_total, 1ull) + 1;
+                    const unsigned long long slot = atomicAdd(&a.stats->bad_claim, 1ull);
+                    if (slot < (unsigned long long)kMaxBadRecords)
+                    {
+                        a.stats->bad_xf[slot] = xf.id;
+#pragma unroll
+                        for (int i = 0; i < D; ++i)
+                            a.stats->bad_pts[slot][i] = as_double(p[i]);
+                    }
+                    if (tot > a.bad_limit)
+                    {
+                        atomicExch(&a.stats->stop, 1u);
+                        stop = true;
+                        break;
+                    }
+                    init();
+                }
+                // extreme coordinates (buffer_renderer.hpp:188-194)
+#pragma unroll
+                for (int i = 0; i < D; ++i)
+                {
+                    ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
+                    ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
+                }
+                // bounds: inclusive [lo, hi]; NaN is out (documented deviation)
+                bool inb = true;
+#pragma unroll
+                for (int i = 0; i < D; ++i)
+                    inb &= (pf[i] >= h.lo[i]) && (pf[i] <= h.hi[i]);
+                if (inb)
+                {
+                    ++s_plot;
+                    uint64_t bi;
+                    if (sizeof(R) == sizeof(double))
+                    {
+                        // buffer_renderer.hpp:200-209
+                        bi = to_index<R>((pf[0] - h.lo[0]) * h.mult_d[0]);
+#pragma unroll
+                        for (int i = 1; i < D; ++i)
+                            bi += to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]) * h.mult_i[i];
+                    }
+                    else
+                    {
+                        // FP32: per-axis index clamped to the axis
+                        bi = 0;
+#pragma unroll
+                        for (int i = 0; i < D; ++i)
+                        {
+                            uint64_t di = to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]);
+                            di = di < h.size[i] ? di : h.size[i] - 1;
+                            bi += di * h.mult_i[i];
+                        }
+                    }
+                    if (bi < h.cells)
+                    {
+                        if (SPILL)
+                        {
+                            const unsigned int old = atomicAdd(&a.counts[bi], 1u);
+                            if (old == 0xFFFFFFFFu)
+                                atomicAdd(&a.hi[bi], 1u);
+                        }
+                        else
+                            atomicAdd(&a.counts[bi], 1u);
+                        if (COLOR)
+                            for (int i = 0; i < r; ++i)
+                                atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));
+                    }
+                    else
+                        ++dropped;
+                }
+                if (((++poll) & kStopPollMask) == 0)
+                {
+                    if (*vstop || (a.cancel && *a.cancel))
+                    {
+                        if (a.cancel && *a.cancel)
+                            atomicExch(&a.stats->cancelled, 1u);
+                        stop = true;
+                        break;
+                    }
+                }
+            }
+        }
+    }
+
+    // merge statistics: warp reduce, then one atomic per warp
+    const unsigned int lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        s_iter += __shfl_down_sync(0xffffffffu, s_iter, off);
+        s_plot += __shfl_down_sync(0xffffffffu, s_plot, off);
+        dropped += __shfl_down_sync(0xffffffffu, dropped, off);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            const R lo = __shfl_down_sync(0xffffffffu, ext_lo[i], off);
+            const R hi = __shfl_down_sync(0xffffffffu, ext_hi[i], off);
+            ext_lo[i] = lo < ext_lo[i] ? lo : ext_lo[i];
+            ext_hi[i] = hi > ext_hi[i] ? hi : ext_hi[i];
+        }
+    }
+    if (lane == 0)
+    {
+        if (s_iter)
+            atomicAdd(&a.stats->s_iter, s_iter);
+        if (s_plot)
+            atomicAdd(&a.stats->s_plot, s_plot);
+        if (dropped)
+            atomicAdd(&a.stats->dropped, dropped);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            if (ext_lo[i] == ext_lo[i] && ext_lo[i] != R(1) / R(0))
+                atomicMin(&a.stats->ext_lo[i], order_key(as_double(ext_lo[i])));
+            if (ext_hi[i] == ext_hi[i] && ext_hi[i] != -R(1) / R(0))
+                atomicMax(&a.stats->ext_hi[i], order_key(as_double(ext_hi[i])));
+        }
+    }
+    __syncthreads();
+    if (local_xfc)
+    {
+        for (int i = 0; i < nxf; ++i)
+        {
+            unsigned long long v = xfc_local[i * BLOCK + threadIdx.x];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+                v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0 && v)
+                atomicAdd(&a.stats->xf_dist[i], v);
+        }
+    }
+    else
+    {
+        for (int i = threadIdx.x; i < nxf; i += BLOCK)
+            if (xfc_shared[i])
+                atomicAdd(&a.stats->xf_dist[i], xfc_shared[i]);
+    }
+}
+
+template <int D, typename R, bool COLOR, bool SPILL, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) chaos_kernel(const RenderArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_program<BLOCK>(smem, a.prog, a.prog_bytes);
+    __syncthreads();
+    chaos_body<D, R, COLOR, SPILL, BLOCK>(a, smem);
+}
+
+// XForm::applyIteration on a batch of points; point k uses stream
+// key(KEY, k), as the reference driver seeds before each point.
+template <int D, typename R>
+__global__ void __launch_bounds__(128) step_kernel(const StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_program<128>(smem, a.prog, a.prog_bytes);
+    __syncthreads();
+    Prog<R> pg;
+    pg.bind(smem);
+    uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
+    DevIsaac<128> rng;
+    rng.mem = ismem + threadIdx.x;
+    rng.rsl = ismem + 16 * 128 + threadIdx.x;
+    const int xi = a.xf_index < 0 ? pg.h->nxf : a.xf_index;
+    for (unsigned long long k = (unsigned long long)blockIdx.x * 128 + threadIdx.x;
+         k < a.npts; k += (unsigned long long)gridDim.x * 128)
+    {
+        rng.seed(stream_key(a.key, k), a.isaac_init);
+        R p[D], q[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            p[i] = (R)a.in[k * D + i];
+        apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            a.out[k * D + i] = (double)q[i];
+    }
+}
+
+// One trajectory from stream key KEY: start, settle, then n samples
+// (xform id and point after each), single thread.
+template <int D, typename R>
+__global__ void trace_kernel(const TraceArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_program<1>(smem, a.prog, a.prog_bytes);
+    __syncthreads();
+    Prog<R> pg;
+    pg.bind(smem);
+    uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
+    DevIsaac<1> rng;
+    rng.mem = ismem;
+    rng.rsl = ismem + 16;
+    rng.seed(a.key, a.isaac_init);
+    using T = RealTraits<R>;
+    R p[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        p[i] = R(2) * T::unit(rng.next()) - R(1);
+    for (unsigned long long k = 0; k < a.settle; ++k)
+    {
+        R q[D];
+        apply_xform<D, R>(pg, pg.xf[pick_xform<R>(pg, rng)], p, q, rng);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            p[i] = q[i];
+    }
+    for (unsigned long long k = 0; k < a.n; ++k)
+    {
+        const int xi = pick_xform<R>(pg, rng);
+        R q[D];
+        apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            p[i] = q[i];
+            a.pts[k * D + i] = (double)q[i];
+        }
+        a.ids[k] = (int)pg.xf[xi].id;
+    }
+}
+
+} // namespace ffr

@@ -1,0 +1,86 @@
+// Device-resident description of one normalised flame ("flame program").
+//
+// Built on the host from the parsed flame (flame.cpp) in the arithmetic type
+// R of the kernel that runs it (double for the FP64 mirror, float for FP32),
+// laid out as one contiguous blob so a CTA copies it into shared memory with
+// a single coalesced loop.  Every thread indexes its own xform per sample, so
+// shared memory (divergent addresses at full rate) is used instead of
+// __constant__ (divergent addresses serialise).
+//
+// Blob layout (all offsets in bytes from the blob start, 16-byte aligned):
+//   ProgHeader<R>
+//   uint64_t thresh[nxf]        xform selection thresholds (see below)
+//   XformT<R> xf[nxf + 1]       sorted xforms, then the final xform
+//   VarT<R>   var[nvar]         variations of all xforms, in xform order
+//   R         color[(nxf+1) * color_dims]
+//
+// Selection: the reference draws r = (w >> 11) / 2^53 (FlameRNG::randNum,
+// src/rng/flame_rng.hpp:67-87) and takes the first i with xfcw[i] >= r
+// (Flame::getRandomXForm, src/types/flame.hpp:212-219).  With m = w >> 11,
+// xfcw[i] < m / 2^53 holds exactly when m > floor(xfcw[i] * 2^53), so
+// thresh[i] = floor(xfcw[i] * 2^53) and the choice is the first i with
+// m <= thresh[i]: the same choice for every word, in integer arithmetic.
+#pragma once
+
+#include <cstdint>
+
+#include "variation_ids.h"
+
+namespace ffr {
+
+constexpr int kMaxDims = 3;          // ffr-buf compiles dims 1..3 (ffr_buf.cpp:134-141)
+constexpr int kMaxColorDims = 127;   // flame.hpp:156
+constexpr int kVarParams = 16;
+constexpr int kMaxXformIds = 4096;
+constexpr int kMaxBadRecords = 4096;
+constexpr uint32_t kMaxProgramBytes = 48 * 1024;
+
+template <typename R>
+struct alignas(16) XformT
+{
+    R pre[kMaxDims * kMaxDims + kMaxDims];   // A row-major, then b
+    R post[kMaxDims * kMaxDims + kMaxDims];
+    R color_speed;
+    uint32_t id;            // index in the JSON xform list (stats are by id)
+    int16_t var_begin;
+    int16_t var_count;
+    uint8_t has_pre;
+    uint8_t has_post;
+    uint8_t has_color;
+    uint8_t pad;
+};
+
+template <typename R>
+struct alignas(16) VarT
+{
+    int32_t type;           // VariationId
+    int16_t axis_x;         // 2-D variations: the plane they act on
+    int16_t axis_y;
+    R weight;
+    R p[kVarParams];        // per-variation parameters (variation_ids.h)
+};
+
+template <typename R>
+struct alignas(16) ProgHeader
+{
+    int32_t dims;
+    int32_t nxf;            // selectable xforms (zero weights removed)
+    int32_t has_final;
+    int32_t color_dims;
+    int32_t nvar;
+    int32_t xform_ids;      // xforms in the JSON (getXFormIDCount)
+    uint32_t off_thresh;
+    uint32_t off_xf;
+    uint32_t off_var;
+    uint32_t off_color;
+    uint32_t total_bytes;
+    uint32_t rng_words_max; // upper bound of RNG words one xform step draws
+    uint64_t size[kMaxDims];
+    uint64_t mult_i[kMaxDims];
+    uint64_t cells;
+    R lo[kMaxDims];
+    R hi[kMaxDims];
+    R mult_d[kMaxDims];     // size/(hi-lo) * (1 - 2^-52)  (buffer_renderer.hpp:126-127)
+};
+
+} // namespace ffr

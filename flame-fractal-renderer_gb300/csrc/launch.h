@@ -1,0 +1,138 @@
+// Interface between the host runtime (api.cpp) and the kernel translation
+// units.  Plain structs shared by host and device code.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "flame_program.h"
+
+namespace ffr {
+
+// Device-side statistics of one render call (the reference's `stats`
+// struct, buffer_renderer.hpp:85-106).  Extremes are stored as order-keys
+// (monotone u64 encodings of doubles) so atomicMin/atomicMax merge them.
+struct DevStats
+{
+    unsigned long long s_iter;
+    unsigned long long s_plot;
+    unsigned long long bad_total;
+    unsigned long long dropped;
+    unsigned long long bad_claim;
+    unsigned int stop;          // bad-value limit exceeded
+    unsigned int cancelled;     // host cancel flag seen
+    unsigned long long ext_lo[kMaxDims];
+    unsigned long long ext_hi[kMaxDims];
+    unsigned long long xf_dist[kMaxXformIds];   // by sorted xform index
+    unsigned long long bad_xf[kMaxBadRecords];  // xform id of each bad value
+    double bad_pts[kMaxBadRecords][kMaxDims];
+};
+
+struct RenderArgs
+{
+    const unsigned char* prog;      // device copy of the program blob
+    unsigned int prog_bytes;
+    int nxf;
+    int color_dims;
+    int spill;                      // counts may pass 2^32: keep high words
+    unsigned long long seed;
+    unsigned long long streams;     // total streams of the job
+    unsigned long long samples;
+    unsigned long long traj_len;
+    unsigned long long settle;
+    unsigned long long bad_limit;
+    unsigned int* counts;           // u32 low words, one per cell
+    unsigned int* hi;               // u32 high words (spill), or null
+    double* colors;                 // cells * color_dims, or null
+    DevStats* stats;
+    const volatile unsigned int* cancel;   // host-mapped cancel flag, or null
+    unsigned long long isaac_init[16];
+};
+
+// Single xform application on a batch of points (one stream per point).
+struct StepArgs
+{
+    const unsigned char* prog;
+    unsigned int prog_bytes;
+    int xf_index;                   // sorted xform index, -1 = final
+    unsigned long long key;
+    unsigned long long npts;
+    const double* in;               // npts * dims
+    double* out;
+    unsigned long long isaac_init[16];
+};
+
+// First n samples of one trajectory (xform ids and points).
+struct TraceArgs
+{
+    const unsigned char* prog;
+    unsigned int prog_bytes;
+    unsigned long long key;
+    unsigned long long settle;
+    unsigned long long n;
+    int* ids;
+    double* pts;                    // n * dims
+    unsigned long long isaac_init[16];
+};
+
+// the 16-word randmem table every stream starts from (isaac64.cuh)
+struct IsaacInit
+{
+    unsigned long long w[16];
+};
+
+// precision: 0 = FP64 mirror, 1 = FP32
+#define FFR_DECLARE_LAUNCHERS(P, D)                                              \
+    cudaError_t launch_render_p##P##_d##D(const RenderArgs&, int grid,          \
+                                          cudaStream_t);                        \
+    cudaError_t occupancy_p##P##_d##D(int color, int spill, int* blocks_per_sm, \
+                                      int* block, unsigned int prog_bytes,      \
+                                      int nxf, size_t* smem);                   \
+    cudaError_t launch_step_p##P##_d##D(const StepArgs&, cudaStream_t);         \
+    cudaError_t launch_trace_p##P##_d##D(const TraceArgs&, cudaStream_t);
+
+FFR_DECLARE_LAUNCHERS(0, 1)
+FFR_DECLARE_LAUNCHERS(0, 2)
+FFR_DECLARE_LAUNCHERS(0, 3)
+FFR_DECLARE_LAUNCHERS(1, 1)
+FFR_DECLARE_LAUNCHERS(1, 2)
+FFR_DECLARE_LAUNCHERS(1, 3)
+
+// buffer_kernels.cu
+cudaError_t launch_isaac_words(unsigned long long key, unsigned long long n,
+                               unsigned long long* out,
+                               const unsigned long long* init16, cudaStream_t);
+cudaError_t launch_accumulate(const unsigned long long* file, unsigned long long cells,
+                              int color_dims, unsigned int* counts, unsigned int* hi,
+                              double* colors, int overwrite, cudaStream_t);
+cudaError_t launch_export(unsigned long long* file, unsigned long long cells,
+                          int color_dims, const unsigned int* counts,
+                          const unsigned int* hi, const double* colors, cudaStream_t);
+cudaError_t launch_file_max(const unsigned long long* file, unsigned long long cells,
+                            int color_dims, unsigned long long* out, cudaStream_t);
+// histogram sum/min/max over counts (+ hi); out[0]=sum, out[1]=min, out[2]=max
+cudaError_t launch_hist_reduce(const unsigned int* counts, const unsigned int* hi,
+                               unsigned long long cells, unsigned long long* out,
+                               cudaStream_t);
+
+cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned int iters,
+                               int grid, int block, unsigned int salt, cudaStream_t);
+
+// monotone u64 key of a double (NaN never stored)
+__host__ __device__ inline unsigned long long order_key(double d)
+{
+    unsigned long long u;
+    memcpy(&u, &d, 8);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+__host__ __device__ inline double key_to_double(unsigned long long k)
+{
+    unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+}
+
+} // namespace ffr

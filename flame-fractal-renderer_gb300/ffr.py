@@ -1,0 +1,303 @@
+"""ctypes binding of libffr_gpu.so (include/ffr_gpu.h).
+
+The Python face of the reference's BufferRenderer<dims> interface
+(src/renderers/buffer_renderer.hpp:254-584): construct from a flame JSON,
+add_buffer / render / write_buffer / histogram, plus the verification entry
+points (isaac_words, step, trace).  All work runs in the CUDA library; if it
+cannot be loaded this module raises instead of computing anything itself.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libffr_gpu.so")
+CLI_PATH = os.path.join(HERE, "_build", "ffr-buf")
+
+FFR_ABI_VERSION = 1
+MAX_DIMS = 3
+MAX_XFORM_IDS = 4096
+MAX_BAD_RECORDS = 4096
+
+FFR_OK, FFR_BAD_VALUES, FFR_ERR_PARSE, FFR_ERR_ARG, FFR_ERR_IO, FFR_ERR_OOM, \
+    FFR_ERR_TIMEOUT, FFR_ERR_CUDA, FFR_ERR_STATE = range(9)
+STATUS_NAMES = ["FFR_OK", "FFR_BAD_VALUES", "FFR_ERR_PARSE", "FFR_ERR_ARG",
+                "FFR_ERR_IO", "FFR_ERR_OOM", "FFR_ERR_TIMEOUT", "FFR_ERR_CUDA",
+                "FFR_ERR_STATE"]
+FP64, FP32 = 0, 1
+
+# every symbol include/ffr_gpu.h declares
+EXPORTS = [
+    "ffr_default_opts", "ffr_create", "ffr_destroy", "ffr_last_error",
+    "ffr_info", "ffr_size", "ffr_flame_json", "ffr_add_buffer", "ffr_render",
+    "ffr_read_buffer", "ffr_load_buffer", "ffr_histogram", "ffr_clear",
+    "ffr_isaac_words", "ffr_step", "ffr_trace", "ffr_plan",
+    "ffr_measure_atomic_rate",
+]
+
+
+class FfrError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES[status] if 0 <= status < 9 else status}: {message}")
+        self.status = status
+        self.message = message
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_uint32), ("device", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("settle", ctypes.c_uint64), ("streams", ctypes.c_uint64),
+                ("traj_len", ctypes.c_uint64), ("timeout_ms", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("samples_iterated", ctypes.c_uint64),
+                ("samples_plotted", ctypes.c_uint64),
+                ("bad_values", ctypes.c_uint64), ("dropped", ctypes.c_uint64),
+                ("ext_lo", ctypes.c_double * MAX_DIMS),
+                ("ext_hi", ctypes.c_double * MAX_DIMS),
+                ("xform_ids", ctypes.c_uint64),
+                ("xf_dist", ctypes.c_uint64 * MAX_XFORM_IDS),
+                ("bad_recorded", ctypes.c_uint64),
+                ("bad_xf", ctypes.c_uint64 * MAX_BAD_RECORDS),
+                ("bad_pts", (ctypes.c_double * MAX_DIMS) * MAX_BAD_RECORDS),
+                ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
+                ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libffr_gpu.so; raises OSError if it is missing (no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise OSError(f"libffr_gpu.so not built at {path}; run "
+                          "__graft_entry__.build() first")
+        L = ctypes.CDLL(path)
+        vp, u64, i32, sz = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_size_t
+        L.ffr_default_opts.argtypes = [ctypes.POINTER(Opts)]
+        L.ffr_default_opts.restype = None
+        L.ffr_create.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts), ctypes.POINTER(vp)]
+        L.ffr_destroy.argtypes = [vp]
+        L.ffr_destroy.restype = None
+        L.ffr_last_error.argtypes = [vp]
+        L.ffr_last_error.restype = ctypes.c_char_p
+        L.ffr_info.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64),
+                               ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(sz)]
+        L.ffr_size.argtypes = [vp, ctypes.POINTER(u64)]
+        L.ffr_flame_json.argtypes = [vp]
+        L.ffr_flame_json.restype = ctypes.c_char_p
+        L.ffr_add_buffer.argtypes = [vp, vp, sz]
+        L.ffr_load_buffer.argtypes = [vp, vp, sz]
+        L.ffr_read_buffer.argtypes = [vp, vp, sz]
+        L.ffr_render.argtypes = [vp, u64, u64, u64, ctypes.POINTER(Stats)]
+        L.ffr_histogram.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                                    ctypes.POINTER(u64)]
+        L.ffr_clear.argtypes = [vp]
+        L.ffr_isaac_words.argtypes = [ctypes.c_int, u64, u64, vp]
+        L.ffr_step.argtypes = [vp, ctypes.c_int, u64, u64, vp, vp]
+        L.ffr_trace.argtypes = [vp, u64, u64, u64, vp, vp]
+        L.ffr_plan.argtypes = [vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
+        L.ffr_measure_atomic_rate.argtypes = [ctypes.c_int, u64, u64,
+                                              ctypes.POINTER(ctypes.c_double)]
+        for name in EXPORTS:
+            f = getattr(L, name)
+            if f.restype is ctypes.c_int:      # default: ffr_status
+                f.restype = ctypes.c_int
+        _lib = L
+        return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(lib, ctx, status: int):
+    if status not in (FFR_OK, FFR_BAD_VALUES):
+        msg = lib.ffr_last_error(ctx).decode("utf-8", "replace")
+        raise FfrError(status, msg)
+    return status
+
+
+@dataclass
+class RenderStats:
+    status: int
+    samples_iterated: int
+    samples_plotted: int
+    bad_values: int
+    dropped: int
+    ext_lo: np.ndarray
+    ext_hi: np.ndarray
+    xf_dist: np.ndarray          # by JSON xform id
+    bad_xf: np.ndarray
+    bad_pts: np.ndarray
+    streams: int
+    traj_len: int
+    settle: int
+    kernel_ms: float
+
+    @property
+    def ok(self) -> bool:
+        return self.status == FFR_OK
+
+
+def isaac_words(key: int, n: int, device: int = 0) -> np.ndarray:
+    """Isaac<u64,4> words after setSeed(key), generated on the GPU."""
+    lib = load_library()
+    out = np.zeros(n, dtype=np.uint64)
+    _check(lib, None, lib.ffr_isaac_words(device, key, n, _ptr(out)))
+    return out
+
+
+def measure_atomic_rate(cells: int, ops: int = 1 << 30, device: int = 0) -> float:
+    """Relaxed u32 atomic adds per second at random cells (roofline peak)."""
+    lib = load_library()
+    out = ctypes.c_double()
+    _check(lib, None, lib.ffr_measure_atomic_rate(device, cells, ops, ctypes.byref(out)))
+    return out.value
+
+
+class BufferRenderer:
+    """GPU BufferRenderer: one flame, one device-resident count buffer."""
+
+    def __init__(self, flame, precision: int = FP64, settle: int = 53,
+                 streams: int = 0, traj_len: int = 0, device: int = 0,
+                 timeout_ms: int = 0):
+        self._lib = load_library()
+        text = flame if isinstance(flame, str) else json.dumps(flame)
+        raw = text.encode("utf-8")
+        o = Opts()
+        self._lib.ffr_default_opts(ctypes.byref(o))
+        o.device, o.precision, o.settle = device, precision, settle
+        o.streams, o.traj_len, o.timeout_ms = streams, traj_len, timeout_ms
+        ctx = ctypes.c_void_p()
+        st = self._lib.ffr_create(raw, len(raw), ctypes.byref(o), ctypes.byref(ctx))
+        if st != FFR_OK:
+            raise FfrError(st, self._lib.ffr_last_error(None).decode("utf-8", "replace"))
+        self._ctx = ctx
+        d, c, r, b = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_size_t()
+        _check(self._lib, self._ctx, self._lib.ffr_info(self._ctx, ctypes.byref(d),
+                                                        ctypes.byref(c), ctypes.byref(r),
+                                                        ctypes.byref(b)))
+        self.dims, self.cells, self.color_dims, self.buffer_bytes = d.value, c.value, r.value, b.value
+        size = (ctypes.c_uint64 * MAX_DIMS)()
+        _check(self._lib, self._ctx, self._lib.ffr_size(self._ctx, size))
+        self.size = [size[i] for i in range(self.dims)]
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.ffr_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def flame_json(self) -> str:
+        return self._lib.ffr_flame_json(self._ctx).decode("utf-8")
+
+    def add_buffer(self, data) -> None:
+        buf = np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray)) \
+            else np.ascontiguousarray(data).view(np.uint8)
+        _check(self._lib, self._ctx, self._lib.ffr_add_buffer(self._ctx, _ptr(buf), buf.nbytes))
+
+    def load_buffer(self, data) -> None:
+        buf = np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray)) \
+            else np.ascontiguousarray(data).view(np.uint8)
+        _check(self._lib, self._ctx, self._lib.ffr_load_buffer(self._ctx, _ptr(buf), buf.nbytes))
+
+    def render(self, samples: int, seed: int, bad_limit: int = 256) -> RenderStats:
+        st = Stats()
+        status = _check(self._lib, self._ctx,
+                        self._lib.ffr_render(self._ctx, samples, seed, bad_limit,
+                                             ctypes.byref(st)))
+        n = self.dims
+        nrec = st.bad_recorded
+        ids = int(st.xform_ids)
+        return RenderStats(
+            status=status, samples_iterated=st.samples_iterated,
+            samples_plotted=st.samples_plotted, bad_values=st.bad_values,
+            dropped=st.dropped, ext_lo=np.array(st.ext_lo[:n]), ext_hi=np.array(st.ext_hi[:n]),
+            xf_dist=np.array(st.xf_dist[:min(ids, MAX_XFORM_IDS)], dtype=np.uint64),
+            bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
+            bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
+            streams=st.streams, traj_len=st.traj_len, settle=st.settle,
+            kernel_ms=st.kernel_ms)
+
+    def plan(self, samples: int):
+        s, L = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib, self._ctx, self._lib.ffr_plan(self._ctx, samples, ctypes.byref(s),
+                                                        ctypes.byref(L)))
+        return s.value, L.value
+
+    def write_buffer(self) -> bytes:
+        out = np.zeros(self.buffer_bytes, dtype=np.uint8)
+        _check(self._lib, self._ctx, self._lib.ffr_read_buffer(self._ctx, _ptr(out), out.nbytes))
+        return out.tobytes()
+
+    def buffer_array(self) -> np.ndarray:
+        """The file layout as a uint64 [cells, 1 + color_dims] array."""
+        out = np.zeros((self.cells, 1 + self.color_dims), dtype=np.uint64)
+        _check(self._lib, self._ctx, self._lib.ffr_read_buffer(self._ctx, _ptr(out), out.nbytes))
+        return out
+
+    def counts(self) -> np.ndarray:
+        return self.buffer_array()[:, 0].copy()
+
+    def histogram(self):
+        s, mn, mx = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib, self._ctx, self._lib.ffr_histogram(self._ctx, ctypes.byref(s),
+                                                             ctypes.byref(mn), ctypes.byref(mx)))
+        return s.value, mn.value, mx.value
+
+    def clear(self) -> None:
+        _check(self._lib, self._ctx, self._lib.ffr_clear(self._ctx))
+
+    def step(self, xf_index: int, key: int, pts: np.ndarray) -> np.ndarray:
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        out = np.zeros_like(pts)
+        _check(self._lib, self._ctx, self._lib.ffr_step(self._ctx, xf_index, key,
+                                                        pts.shape[0], _ptr(pts), _ptr(out)))
+        return out
+
+    def trace(self, key: int, settle: int, n: int):
+        ids = np.zeros(n, dtype=np.int32)
+        pts = np.zeros((n, self.dims), dtype=np.float64)
+        _check(self._lib, self._ctx, self._lib.ffr_trace(self._ctx, key, settle, n,
+                                                         _ptr(ids), _ptr(pts)))
+        return ids, pts
+
+
+def create_status(flame_text: str, precision: int = FP64):
+    """(status, message) of ffr_create without keeping the context."""
+    lib = load_library()
+    raw = flame_text.encode("utf-8")
+    o = Opts()
+    lib.ffr_default_opts(ctypes.byref(o))
+    o.precision = precision
+    ctx = ctypes.c_void_p()
+    st = lib.ffr_create(raw, len(raw), ctypes.byref(o), ctypes.byref(ctx))
+    msg = lib.ffr_last_error(None).decode("utf-8", "replace")
+    if st == FFR_OK:
+        lib.ffr_destroy(ctx)
+    return st, msg

@@ -1,0 +1,110 @@
+"""Seeded generators of flame JSON documents (the benchmark workloads).
+
+Each function returns a dict in the reference's flame JSON format
+(FLAME_JSON.md of the reference project).  Randomness comes from numpy's
+PCG64 generator seeded explicitly, so the same seed gives the same flame on
+every machine.
+
+  sierpinski_2d      3 xforms, weight 1/3, A = 0.5 I, b = 0.5 v_i with
+                     v = (0,1), (-1,-1), (1,-1); linear; bounds [-1,1]^2
+  tetrahedron_3d     4 xforms, weight 0.25, A = 0.5 I, b = 0.5 v_i with v_i
+                     the vertices (1,1,1), (1,-1,-1), (-1,1,-1), (-1,-1,1)
+  random_2d          k xforms, weights Dirichlet(1); pre-affine entries
+                     U[-1,1]; post-affine identity + N(0, 0.1); 2 variations
+                     per xform drawn without replacement from TIER_A with
+                     weights Dirichlet(1); bounds [-2,2] x [-1.125,1.125]
+  random_3d          the 3-D analogue (2-D variations act on a random plane,
+                     given by axis_x / axis_y)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+TIER_A = ["linear", "sinusoidal", "spherical", "swirl", "horseshoe", "polar", "julia"]
+TWO_D = {"swirl", "horseshoe", "polar", "julia"}
+
+
+def _f(x) -> float:
+    return float(x)
+
+
+def sierpinski_2d(size=(1024, 1024)) -> dict:
+    verts = [(0.0, 1.0), (-1.0, -1.0), (1.0, -1.0)]
+    xfs = []
+    for v in verts:
+        xfs.append({
+            "weight": 1.0 / 3.0,
+            "variations": [{"name": "linear", "weight": 1.0}],
+            "pre_affine": {"A": [[0.5, 0.0], [0.0, 0.5]], "b": [0.5 * v[0], 0.5 * v[1]]},
+        })
+    return {"dimensions": 2, "size": list(size), "bounds": [[-1.0, 1.0], [-1.0, 1.0]],
+            "xforms": xfs}
+
+
+def tetrahedron_3d(size=(512, 512, 512)) -> dict:
+    verts = [(1, 1, 1), (1, -1, -1), (-1, 1, -1), (-1, -1, 1)]
+    xfs = []
+    for v in verts:
+        xfs.append({
+            "weight": 0.25,
+            "variations": [{"name": "linear", "weight": 1.0}],
+            "pre_affine": {"A": [[0.5, 0, 0], [0, 0.5, 0], [0, 0, 0.5]],
+                           "b": [0.5 * v[0], 0.5 * v[1], 0.5 * v[2]]},
+        })
+    return {"dimensions": 3, "size": list(size),
+            "bounds": [[-1.0, 1.0], [-1.0, 1.0], [-1.0, 1.0]], "xforms": xfs}
+
+
+def random_2d(seed: int, k: int = 6, size=(1920, 1080), variations=TIER_A,
+              nvars: int = 2, bounds=((-2.0, 2.0), (-1.125, 1.125))) -> dict:
+    g = np.random.Generator(np.random.PCG64(seed))
+    w = g.dirichlet(np.ones(k))
+    xfs = []
+    for i in range(k):
+        pre = g.uniform(-1.0, 1.0, size=(2, 3))
+        post = np.eye(2) + g.normal(0.0, 0.1, size=(2, 2))
+        postb = g.normal(0.0, 0.1, size=2)
+        names = list(g.choice(len(variations), size=nvars, replace=False))
+        vw = g.dirichlet(np.ones(nvars))
+        xfs.append({
+            "weight": _f(w[i]),
+            "variations": [{"name": variations[n], "weight": _f(vw[j])}
+                           for j, n in enumerate(names)],
+            "pre_affine": {"A": [[_f(pre[0, 0]), _f(pre[0, 1])], [_f(pre[1, 0]), _f(pre[1, 1])]],
+                           "b": [_f(pre[0, 2]), _f(pre[1, 2])]},
+            "post_affine": {"A": [[_f(post[0, 0]), _f(post[0, 1])],
+                                  [_f(post[1, 0]), _f(post[1, 1])]],
+                            "b": [_f(postb[0]), _f(postb[1])]},
+        })
+    return {"dimensions": 2, "size": list(size),
+            "bounds": [list(bounds[0]), list(bounds[1])], "xforms": xfs}
+
+
+def random_3d(seed: int, k: int = 4, size=(256, 256, 256), variations=TIER_A,
+              nvars: int = 2) -> dict:
+    g = np.random.Generator(np.random.PCG64(seed))
+    w = g.dirichlet(np.ones(k))
+    xfs = []
+    for i in range(k):
+        pre = g.uniform(-1.0, 1.0, size=(3, 4))
+        post = np.eye(3) + g.normal(0.0, 0.1, size=(3, 3))
+        postb = g.normal(0.0, 0.1, size=3)
+        names = list(g.choice(len(variations), size=nvars, replace=False))
+        vw = g.dirichlet(np.ones(nvars))
+        vs = []
+        for j, n in enumerate(names):
+            v = {"name": variations[n], "weight": _f(vw[j])}
+            if variations[n] in TWO_D:
+                ax = g.choice(3, size=2, replace=False)
+                v["axis_x"], v["axis_y"] = int(ax[0]), int(ax[1])
+            vs.append(v)
+        xfs.append({
+            "weight": _f(w[i]),
+            "variations": vs,
+            "pre_affine": {"A": [[_f(pre[r, c]) for c in range(3)] for r in range(3)],
+                           "b": [_f(pre[r, 3]) for r in range(3)]},
+            "post_affine": {"A": [[_f(post[r, c]) for c in range(3)] for r in range(3)],
+                            "b": [_f(postb[r]) for r in range(3)]},
+        })
+    return {"dimensions": 3, "size": list(size),
+            "bounds": [[-2.0, 2.0], [-2.0, 2.0], [-2.0, 2.0]], "xforms": xfs}

@@ -1,0 +1,198 @@
+/*
+ * ffr_gpu.h -- C ABI of the GB300 chaos-game buffer generator
+ * (libffr_gpu.so).  Plain pointers, sizes and status codes; no C++ types and
+ * no exceptions cross this boundary.
+ *
+ * It replaces the reference's in-process C++ interface of the ffr-buf path:
+ *   BufferRenderer<dims>(Flame(Json))      src/renderers/buffer_renderer.hpp:254-256
+ *   BufferRenderer::addBuffer(istream&)    src/renderers/buffer_renderer.hpp:419-452
+ *   BufferRenderer::render(...)            src/renderers/buffer_renderer.hpp:269-338
+ *   BufferRenderer::renderSeeded(...)      src/renderers/buffer_renderer.hpp:349-372
+ *   BufferRenderer::writeBuffer(ostream&)  src/renderers/buffer_renderer.hpp:476-480
+ *   BufferRenderer::histogramSum/Min/Max   src/renderers/buffer_renderer.hpp:483-507
+ *   stats getters                          src/renderers/buffer_renderer.hpp:509-584
+ * and its caller, run_renderer<dims>() in src/ffr_buf.cpp:146-274.
+ *
+ * Buffer bytes are the reference file layout: for each cell (x fastest, then
+ * y rows, then z planes) one u64 count followed by color_dims f64 colour
+ * sums, native (little) endian, no header.
+ *
+ * Threading: one context per host thread, or external locking.  Device work
+ * runs on a stream owned by the context; every call returns after its work
+ * has finished (or reports FFR_ERR_TIMEOUT) unless stated otherwise.
+ */
+#ifndef FFR_GPU_H
+#define FFR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFR_ABI_VERSION 1
+
+typedef enum ffr_status {
+    FFR_OK = 0,
+    /* bad-value limit exceeded; buffer and stats are still valid and the
+       reference CLI still writes its output and exits 0 (ffr_buf.cpp:228-230) */
+    FFR_BAD_VALUES = 1,
+    FFR_ERR_PARSE = 2,    /* JSON or flame validation error (JsonError) */
+    FFR_ERR_ARG = 3,      /* invalid argument (runtime_error in render()) */
+    FFR_ERR_IO = 4,       /* short or mismatched buffer ("error reading file") */
+    FFR_ERR_OOM = 5,      /* device memory admission failed */
+    FFR_ERR_TIMEOUT = 6,  /* a bounded wait ran out */
+    FFR_ERR_CUDA = 7,     /* CUDA runtime error */
+    FFR_ERR_STATE = 8     /* call not valid in the context's current state */
+} ffr_status;
+
+typedef enum ffr_precision {
+    /* mirror of the reference's double arithmetic (num_t = double,
+       src/types/types.hpp:29), no FMA contraction */
+    FFR_FP64 = 0,
+    /* FP32 iteration; xform choices and RNG draws still exact per stream */
+    FFR_FP32 = 1
+} ffr_precision;
+
+typedef struct ffr_opts {
+    uint32_t abi_version;      /* FFR_ABI_VERSION */
+    int32_t device;            /* CUDA device ordinal */
+    int32_t precision;         /* ffr_precision */
+    int32_t reserved0;
+    /* iterations discarded at each trajectory start; the reference uses
+       settle_iters<double> = 53 (src/types/constants.hpp:41-47) */
+    uint64_t settle;
+    /* independent ISAAC streams run concurrently (one per GPU thread);
+       0 = choose from the device (SMs x resident threads) */
+    uint64_t streams;
+    /* samples per trajectory (the reference's batch size, one
+       RenderIterator per batch, buffer_renderer.hpp:155); 0 = N / streams */
+    uint64_t traj_len;
+    /* wall-clock limit in ms for any single device wait; 0 = none */
+    uint64_t timeout_ms;
+} ffr_opts;
+
+#define FFR_MAX_DIMS 3
+#define FFR_MAX_XFORM_IDS 4096
+#define FFR_MAX_BAD_RECORDS 4096
+
+typedef struct ffr_stats {
+    uint64_t samples_iterated;   /* getSamplesIterated */
+    uint64_t samples_plotted;    /* getSamplesPlotted */
+    uint64_t bad_values;         /* getBadValueXForms().size() */
+    uint64_t dropped;            /* in-bounds points whose index fell past the
+                                    last cell (undefined in the reference) */
+    double ext_lo[FFR_MAX_DIMS]; /* getPointExtremes */
+    double ext_hi[FFR_MAX_DIMS];
+    uint64_t xform_ids;          /* getXFormIDCount */
+    uint64_t xf_dist[FFR_MAX_XFORM_IDS];   /* getXFormDistribution */
+    uint64_t bad_recorded;       /* entries filled in bad_xf / bad_pts */
+    uint64_t bad_xf[FFR_MAX_BAD_RECORDS];  /* getBadValueXForms (first ones) */
+    double bad_pts[FFR_MAX_BAD_RECORDS][FFR_MAX_DIMS];  /* getBadValuePoints */
+    /* launch parameters actually used */
+    uint64_t streams;
+    uint64_t traj_len;
+    uint64_t settle;
+    double kernel_ms;            /* device time of the render kernel(s) */
+} ffr_stats;
+
+typedef struct ffr_ctx ffr_ctx;
+
+/* Fill *opts with defaults (device 0, FP64, settle 53, auto streams). */
+void ffr_default_opts(ffr_opts *opts);
+
+/* Parse and validate a flame (JSON text, comments allowed), allocate the
+   zeroed count/colour buffer on the device.  Replaces Flame<dims>(Json) +
+   BufferRenderer<dims>(flame).  On failure *out is NULL and
+   ffr_last_error(NULL) holds the message. */
+ffr_status ffr_create(const char *json, size_t len, const ffr_opts *opts,
+                      ffr_ctx **out);
+
+void ffr_destroy(ffr_ctx *ctx);
+
+/* Message of the last failing call on ctx (or of the last failing
+   ffr_create on this thread when ctx is NULL).  Never NULL. */
+const char *ffr_last_error(const ffr_ctx *ctx);
+
+/* Geometry of the context's buffer. */
+ffr_status ffr_info(const ffr_ctx *ctx, uint32_t *dims, uint64_t *cells,
+                    uint32_t *color_dims, size_t *buffer_bytes);
+
+/* Buffer size per dimension (Flame::getSize, src/types/flame.hpp:221-224);
+   size must hold `dims` entries. */
+ffr_status ffr_size(const ffr_ctx *ctx, uint64_t *size);
+
+/* The parsed flame as compact JSON (the CLI's "flame:" echo,
+   src/ffr_buf.cpp:130).  Owned by ctx. */
+const char *ffr_flame_json(const ffr_ctx *ctx);
+
+/* Add a buffer in the file layout (addBuffer, buffer_renderer.hpp:419-452):
+   u64 counts add as integers, f64 colours add as doubles.  bytes must be at
+   least the buffer size (extra trailing bytes are ignored, as a stream with
+   more data is); a shorter input is FFR_ERR_IO and leaves the buffer
+   unchanged. */
+ffr_status ffr_add_buffer(ffr_ctx *ctx, const void *cells, size_t bytes);
+
+/* Render `samples` post-settle samples (render()/renderSeeded()).  Stream s
+   of `seed` is Isaac<u64,4> seeded with setSeed(seed + fmix64(s)).
+   bad_limit is the reference's -z (default 256).  stats may be NULL. */
+ffr_status ffr_render(ffr_ctx *ctx, uint64_t samples, uint64_t seed,
+                      uint64_t bad_limit, ffr_stats *stats);
+
+/* Copy the buffer out in the file layout (writeBuffer).  bytes must be at
+   least the buffer size. */
+ffr_status ffr_read_buffer(ffr_ctx *ctx, void *cells, size_t bytes);
+
+/* Overwrite the buffer from the file layout (readBuffer). */
+ffr_status ffr_load_buffer(ffr_ctx *ctx, const void *cells, size_t bytes);
+
+/* histogramSum / histogramMin / histogramMax over the count channel. */
+ffr_status ffr_histogram(ffr_ctx *ctx, uint64_t *sum, uint64_t *min,
+                         uint64_t *max);
+
+/* Zero the buffer (a fresh BufferRenderer). */
+ffr_status ffr_clear(ffr_ctx *ctx);
+
+/* ---------------------------------------------------------------------
+ * Verification entry points: the same device code as ffr_render, exposed
+ * one function at a time so each can be checked against the reference.
+ * ------------------------------------------------------------------- */
+
+/* n words of Isaac<u64,4> after setSeed(key): Isaac::next()
+   (src/rng/isaac.hpp:321-329, seeding 267-282), generated on the device of
+   `device`. */
+ffr_status ffr_isaac_words(int device, uint64_t key, uint64_t n, uint64_t *out);
+
+/* XForm::applyIteration (src/types/xform.hpp:211-227) of sorted xform
+   `xf_index` (0 = largest weight; -1 = final xform) applied to npts points
+   (dims doubles each); point k draws from stream key + fmix64(k).  Runs in
+   the context's precision; results are returned as doubles. */
+ffr_status ffr_step(ffr_ctx *ctx, int xf_index, uint64_t key, uint64_t npts,
+                    const double *in, double *out);
+
+/* One trajectory (RenderIterator, src/renderers/render_iterator.hpp:52-139)
+   from setSeed(key): random start, `settle` discarded iterations, then n
+   iterations; ids[k] = chosen xform id, pts[k*dims..] = point after it. */
+ffr_status ffr_trace(ffr_ctx *ctx, uint64_t key, uint64_t settle, uint64_t n,
+                     int32_t *ids, double *pts);
+
+/* Launch configuration ffr_render would use for `samples` (streams and
+   trajectory length after defaults are applied). */
+ffr_status ffr_plan(ffr_ctx *ctx, uint64_t samples, uint64_t *streams,
+                    uint64_t *traj_len);
+
+/* ---------------------------------------------------------------------
+ * Measurement (no counterpart in the reference): the roofline denominator
+ * of the binning step.  Issues `ops` relaxed 4-byte atomic adds at uniformly
+ * random cells of a zeroed `cells`-cell u32 buffer on `device` and reports
+ * the achieved rate (one warm-up launch, one timed launch, CUDA events).
+ * ------------------------------------------------------------------- */
+ffr_status ffr_measure_atomic_rate(int device, uint64_t cells, uint64_t ops,
+                                   double *ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFR_GPU_H */

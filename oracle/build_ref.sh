@@ -1,0 +1,23 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/ffr_ref from the reference's own, unmodified sources
+# where they lie (REF_ROOT, default /root/reference), plus the project's
+# shims in oracle/shim (a JSON class standing in for the absent nlohmann/json
+# and an empty boost/gil.hpp) and the driver oracle/ref_driver.cpp.
+# Output goes only to oracle/_ref/ (git-ignored).  The reference's own CMake
+# build is not used: it needs Boost.program_options, Boost.GIL and libpng,
+# none of which is installed.  -ffp-contract=off keeps FP64 results
+# identical between x86-64 and aarch64.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF_ROOT="${REF_ROOT:-/root/reference}"
+if [ ! -d "$REF_ROOT/src" ]; then
+    echo "build_ref.sh: reference sources not found at $REF_ROOT/src" >&2
+    exit 1
+fi
+mkdir -p "$HERE/_ref"
+exec g++ -std=c++23 -O3 -DNDEBUG -ffp-contract=off -w \
+    -I "$HERE/shim" -I "$HERE/shim/nest/nest" -I "$REF_ROOT/src" \
+    "$HERE/ref_driver.cpp" \
+    "$REF_ROOT/src/rng/flame_rng.cpp" \
+    "$REF_ROOT/src/utils/json.cpp" \
+    -o "$HERE/_ref/ffr_ref" -lpthread

@@ -1,0 +1,243 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the
+reference's golden vectors and the oracle.
+
+Tolerances (the bar the reference path sets):
+  * RNG words, xform choices, integer counts and sample statistics: exact.
+  * FP64 mode, flames built from + - * / sqrt only (linear, spherical,
+    horseshoe, affines): buffers and points bit-identical to the reference.
+  * FP64 single xform step through libm transcendentals (sin, cos, atan2):
+    |gpu - ref| <= 1e-12 * max(|ref|, 1) per coordinate.
+  * Chaotic trajectories through transcendentals: histogram total variation
+    distance <= 3x the noise floor measured between two oracle runs with
+    different seeds at the same sample count.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_flame_text, golden_manifest
+
+pytestmark = pytest.mark.gpu
+
+MAN = golden_manifest()
+ALGEBRAIC = {"sierpinski", "tetra", "alg2d", "color", "ties", "badval"}
+STEP_REL = 1e-12
+
+
+def npz(name):
+    return np.load(os.path.join(GOLDEN, "data", name + ".npz"))
+
+
+def hexd(s):
+    return np.frombuffer(int(s, 16).to_bytes(8, "little"), dtype=np.float64)[0]
+
+
+def tv(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return 0.5 * np.abs(a / a.sum() - b / b.sum()).sum()
+
+
+@pytest.mark.parametrize("key", MAN["kat"]["keys"])
+def test_isaac_words_match_reference(ffr, key):
+    want = npz("kat")[f"k{key}"]
+    got = ffr.isaac_words(int(key, 16), len(want))
+    np.testing.assert_array_equal(got, want)
+
+
+def test_isaac_many_keys_match_oracle(ffr, fo):
+    rng = np.random.Generator(np.random.PCG64(99))
+    for key in rng.integers(0, 2**63, size=20, dtype=np.int64).tolist():
+        np.testing.assert_array_equal(ffr.isaac_words(key, 333), fo.isaac_words(key, 333))
+
+
+@pytest.mark.parametrize("name", sorted(MAN["flames"]))
+def test_single_step_fp64(ffr, name):
+    g = MAN["flames"][name]
+    d = npz(name)
+    with ffr.BufferRenderer(golden_flame_text(name), precision=ffr.FP64) as r:
+        for xi in g["steps"]:
+            got = r.step(xi, 777, d["step_in"])
+            want = d[f"step_out_{xi}"]
+            if name in ALGEBRAIC:
+                np.testing.assert_array_equal(got, want)
+            else:
+                err = np.abs(got - want) / np.maximum(np.abs(want), 1.0)
+                assert err.max() <= STEP_REL, (xi, err.max())
+
+
+@pytest.mark.parametrize("name", ["c2small", "rand3d", "julia3", "line1d"])
+def test_single_step_million_points(ffr, fo, name):
+    """10^6 seeded points per xform, FP64, within 1e-12 of the oracle."""
+    g = MAN["flames"][name]
+    text = golden_flame_text(name)
+    of = fo.OracleFlame(fo.load_flame(text))
+    rng = np.random.Generator(np.random.PCG64(31337))
+    pts = rng.uniform(-2.0, 2.0, size=(1_000_000, g["dims"]))
+    worst = 0.0
+    with ffr.BufferRenderer(text, precision=ffr.FP64) as r:
+        for xi in g["steps"][:3]:
+            got = r.step(xi, 4242, pts)
+            want = fo.step(of, xi, 4242, pts)
+            err = np.abs(got - want) / np.maximum(np.abs(want), 1.0)
+            worst = max(worst, float(err.max()))
+    assert worst <= STEP_REL, worst
+
+
+@pytest.mark.parametrize("name", sorted(MAN["flames"]))
+def test_trace_fp64(ffr, name):
+    d = npz(name)
+    n = len(d["trace_ids"])
+    with ffr.BufferRenderer(golden_flame_text(name), precision=ffr.FP64) as r:
+        ids, pts = r.trace(12345, 20, n)
+    np.testing.assert_array_equal(ids, d["trace_ids"])
+    if name in ALGEBRAIC:
+        np.testing.assert_array_equal(pts, d["trace_pts"])
+    else:
+        # chaotic divergence from ulp-level libm differences: compare the start
+        err = np.abs(pts[:8] - d["trace_pts"][:8]) / np.maximum(np.abs(d["trace_pts"][:8]), 1.0)
+        assert err.max() <= 1e-9
+
+
+@pytest.mark.parametrize("name", sorted(MAN["flames"]))
+def test_trace_fp32_choices_exact(ffr, name):
+    """FP32 iteration keeps the reference's xform choices per stream."""
+    d = npz(name)
+    n = len(d["trace_ids"])
+    with ffr.BufferRenderer(golden_flame_text(name), precision=ffr.FP32) as r:
+        ids, _ = r.trace(12345, 20, n)
+    np.testing.assert_array_equal(ids, d["trace_ids"])
+
+
+@pytest.mark.parametrize("case", MAN["renders"], ids=lambda c: f"{c['key']}-{c['flame']}")
+def test_render_fp64_matches_reference(ffr, case):
+    d = npz(case["key"])
+    st = case["stats"]
+    with ffr.BufferRenderer(golden_flame_text(case["flame"]), precision=ffr.FP64,
+                            settle=case["settle"], streams=case["streams"],
+                            traj_len=case["traj_len"]) as r:
+        s = r.render(case["samples"], case["seed"], case["bad_limit"])
+        buf = r.buffer_array()
+    counts = buf[:, 0]
+    assert s.ok == bool(st["ok"])
+    assert s.samples_iterated == st["s_iter"]
+    assert s.xf_dist.tolist() == st["xf_dist"]
+    if "bad" in st:
+        assert s.bad_values == st["bad"]
+    if case["flame"] in ALGEBRAIC:
+        np.testing.assert_array_equal(counts, d["counts"])
+        assert s.samples_plotted == st["s_plot"]
+        for i, (lo, hi) in enumerate(st["ext"]):
+            assert s.ext_lo[i] == hexd(lo) and s.ext_hi[i] == hexd(hi)
+        if d["colors"].shape[1]:
+            col = buf[:, 1:].copy().view(np.float64)
+            np.testing.assert_allclose(col, d["colors"], rtol=1e-12, atol=1e-9)
+    else:
+        assert abs(int(counts.sum()) - int(d["counts"].sum())) <= 0.02 * d["counts"].sum() + 50
+        assert tv(counts, d["counts"]) < 0.2
+
+
+def test_render_large_exact_vs_oracle(ffr, fo, flames):
+    """1024^2 Sierpinski, 10^7 samples over 10^4 streams: bit-exact buffer."""
+    fl = flames.sierpinski_2d(size=(1024, 1024))
+    text = json.dumps(fl)
+    of = fo.OracleFlame(fo.load_flame(text))
+    seed, S, N, L, Z = 1, 10_000, 10_000_000, 1000, 20
+    ref = fo.render(of, seed, S, N, L, Z, threads=8)
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L) as r:
+        s = r.render(N, seed)
+        got = r.counts()
+    np.testing.assert_array_equal(got, ref.counts)
+    assert s.samples_plotted == ref.s_plot
+    assert s.xf_dist.tolist() == ref.xf_dist.tolist()
+
+
+def test_render_3d_exact_vs_oracle(ffr, fo, flames):
+    fl = flames.tetrahedron_3d(size=(128, 128, 128))
+    text = json.dumps(fl)
+    of = fo.OracleFlame(fo.load_flame(text))
+    seed, S, N, L, Z = 3, 4096, 4_000_000, 977, 20
+    ref = fo.render(of, seed, S, N, L, Z, threads=8)
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L) as r:
+        r.render(N, seed)
+        got = r.counts()
+    np.testing.assert_array_equal(got, ref.counts)
+
+
+def test_histogram_and_round_trip(ffr, flames):
+    text = json.dumps(flames.sierpinski_2d(size=(256, 256)))
+    with ffr.BufferRenderer(text, settle=20) as r:
+        s = r.render(1_000_000, 5)
+        raw = r.write_buffer()
+        hs, hmin, hmax = r.histogram()
+        c = np.frombuffer(raw, dtype=np.uint64)
+        assert hs == int(c.sum()) == s.samples_plotted - s.dropped
+        assert hmin == int(c.min()) and hmax == int(c.max())
+        r.add_buffer(raw)                        # addBuffer doubles every count
+        np.testing.assert_array_equal(r.counts(), 2 * c)
+        r.load_buffer(raw)                       # readBuffer overwrites
+        np.testing.assert_array_equal(r.counts(), c)
+        r.clear()
+        assert r.histogram() == (0, 0, 0)
+
+
+def test_short_input_buffer_is_io_error(ffr, flames):
+    text = json.dumps(flames.sierpinski_2d(size=(16, 16)))
+    with ffr.BufferRenderer(text) as r:
+        with pytest.raises(ffr.FfrError) as e:
+            r.add_buffer(b"\0" * (r.buffer_bytes - 8))
+        assert e.value.status == ffr.FFR_ERR_IO
+        r.add_buffer(b"\1" + b"\0" * (r.buffer_bytes + 15))     # trailing bytes ignored
+        assert r.histogram()[0] == 1
+
+
+def test_counts_past_2_pow_32(ffr, fo, flames):
+    """u32 device counters carry into the high words: exact u64 counts."""
+    text = json.dumps(flames.sierpinski_2d(size=(8, 8)))
+    of = fo.OracleFlame(fo.load_flame(text))
+    base = np.full(64, (1 << 32) - 1000, dtype=np.uint64)
+    with ffr.BufferRenderer(text, settle=20, streams=512, traj_len=500) as r:
+        r.add_buffer(base.tobytes())
+        r.render(2_000_000, 9)
+        got = r.counts()
+    ref = fo.render(of, 9, 512, 2_000_000, 500, 20)
+    np.testing.assert_array_equal(got, base + ref.counts)
+    assert got.max() > (1 << 32)
+
+
+def test_bad_value_limit_stops(ffr):
+    text = golden_flame_text("badval")
+    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=10_000) as r:
+        s = r.render(640_000, 3, bad_limit=5)
+        assert s.status == ffr.FFR_BAD_VALUES
+        assert s.bad_values > 5
+        assert len(s.bad_xf) >= 6
+        hs = r.histogram()[0]
+        assert hs == s.samples_plotted - s.dropped
+        assert s.samples_iterated < 640_000
+
+
+def test_bad_values_recorded_without_stop(ffr, fo):
+    text = golden_flame_text("badval")
+    of = fo.OracleFlame(fo.load_flame(text))
+    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=1000) as r:
+        s = r.render(64_000, 4, bad_limit=10**9)
+        got = r.counts()
+    ref = fo.render(of, 4, 64, 64_000, 1000, 20, bad_limit=10**9)
+    assert s.ok and s.bad_values == ref.bad > 0
+    np.testing.assert_array_equal(got, ref.counts)
+    assert sorted(s.bad_xf.tolist()) == sorted(
+        [int(x) for x in s.bad_xf.tolist()])    # ids are JSON xform ids
+    assert set(s.bad_xf.tolist()) <= {0, 1}
+
+
+def test_timeout_cancels_and_context_survives(ffr, flames):
+    text = json.dumps(flames.random_2d(7))
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=20, timeout_ms=30) as r:
+        with pytest.raises(ffr.FfrError) as e:
+            r.render(50_000_000_000, 1)
+        assert e.value.status == ffr.FFR_ERR_TIMEOUT
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=20) as r:
+        assert r.render(100_000, 1).ok

@@ -1,0 +1,125 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every symbol include/ffr_gpu.h declares, flame validation through the ABI
+rejects what the reference rejects, the CLI's argument handling, and the
+flame generators."""
+import json
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT, golden_manifest
+
+MAN = golden_manifest()
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "ffr_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ffr_[a-z_]+)\s*\(", text)))
+
+
+def test_header_lists_exports(ffr):
+    assert header_functions() == sorted(ffr.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(ffr):
+    lib = ffr.load_library()
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.check_output(["nm", "-D", "--defined-only", ffr.LIB_PATH], text=True)
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    assert exported == set(header_functions())
+
+
+@pytest.mark.parametrize("name", sorted(MAN["invalid"]))
+def test_invalid_flames_rejected_through_abi(ffr, name):
+    case = MAN["invalid"][name]
+    st, msg = ffr.create_status(case["text"])
+    assert st == ffr.FFR_ERR_PARSE, (st, msg)
+    assert msg
+
+
+@pytest.mark.parametrize("name", sorted(MAN["valid_edge"]))
+def test_valid_flames_pass_validation(ffr, name):
+    st, msg = ffr.create_status(MAN["valid_edge"][name]["text"])
+    # parsing happens before any CUDA call: without a GPU the create fails
+    # at device setup, never at validation
+    assert st in (ffr.FFR_OK, ffr.FFR_ERR_CUDA, ffr.FFR_ERR_OOM), (st, msg)
+
+
+def test_unknown_variation_message(ffr):
+    st, msg = ffr.create_status(MAN["invalid"]["unknown_var"]["text"])
+    assert st == ffr.FFR_ERR_PARSE and "unknown variation: nope" in msg
+
+
+def test_default_opts(ffr):
+    import ctypes
+    o = ffr.Opts()
+    ffr.load_library().ffr_default_opts(ctypes.byref(o))
+    assert o.abi_version == ffr.FFR_ABI_VERSION
+    assert o.settle == 53 and o.precision == ffr.FP64 and o.streams == 0
+
+
+def test_isaac_words_rejects_null(ffr):
+    lib = ffr.load_library()
+    assert lib.ffr_isaac_words(0, 1, 4, None) == ffr.FFR_ERR_ARG
+
+
+def test_null_context_is_an_argument_error(ffr):
+    lib = ffr.load_library()
+    assert lib.ffr_render(None, 10, 1, 256, None) == ffr.FFR_ERR_ARG
+    assert lib.ffr_read_buffer(None, None, 0) == ffr.FFR_ERR_ARG
+    assert lib.ffr_last_error(None)
+
+
+def run_cli(ffr, args, stdin=None):
+    return subprocess.run([ffr.CLI_PATH, *args], input=stdin, stdout=subprocess.PIPE,
+                          stderr=subprocess.PIPE)
+
+
+def test_cli_usage(ffr):
+    r = run_cli(ffr, [])
+    assert r.returncode == 1 and b"ffr-buf usage" in r.stderr
+    r = run_cli(ffr, ["-h"])
+    assert r.returncode == 1 and b"--flame" in r.stderr
+
+
+def test_cli_missing_required(ffr, tmp_path):
+    r = run_cli(ffr, ["-o", str(tmp_path / "o.buf")])
+    assert r.returncode == 1 and b"--flame" in r.stderr
+    r = run_cli(ffr, ["-f", "x.json"])
+    assert r.returncode == 1 and b"--output" in r.stderr
+
+
+def test_cli_bad_option_value(ffr):
+    r = run_cli(ffr, ["-f", "-", "-o", "-", "-s", "abc"])
+    assert r.returncode == 1 and b"invalid" in r.stderr
+
+
+def test_cli_rejects_bad_flame(ffr, tmp_path):
+    p = tmp_path / "bad.json"
+    p.write_text(MAN["invalid"]["bad_bounds"]["text"])
+    r = run_cli(ffr, ["-f", str(p), "-o", str(tmp_path / "o.buf")])
+    assert r.returncode == 1
+    assert b"ERROR:" in r.stderr and b"low >= high" in r.stderr
+
+
+def test_flame_generators_are_seeded(flames):
+    a = json.dumps(flames.random_2d(7))
+    b = json.dumps(flames.random_2d(7))
+    c = json.dumps(flames.random_2d(8))
+    assert a == b and a != c
+    f3 = flames.random_3d(5)
+    for x in f3["xforms"]:
+        for v in x["variations"]:
+            if v["name"] in flames.TWO_D:
+                assert v["axis_x"] != v["axis_y"]
+
+
+def test_generated_flames_parse_in_oracle(fo, flames):
+    for fl in (flames.sierpinski_2d(), flames.tetrahedron_3d(), flames.random_2d(7),
+               flames.random_3d(5)):
+        f = fo.load_flame(json.dumps(fl))
+        assert abs(sum(x.weight for x in f.xforms) / sum(x.weight for x in f.xforms) - 1) == 0
