@@ -76,9 +76,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
             jobs.append((obj, [src] + hdrs,
                          [nvcc, *nv_common, *extra, f"-DFFR_P={p}", f"-DFFR_D={d}",
                           "-c", src, "-o", obj]))
-    src = os.path.join(CSRC, "buffer_kernels.cu")
-    obj = os.path.join(OUT, "buffer_kernels.o")
-    jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
+    for name in ("buffer_kernels", "noalloc"):
+        src = os.path.join(CSRC, name + ".cu")
+        obj = os.path.join(OUT, name + ".o")
+        jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
     for name in ("api", "flame", "json", "variations_host"):
         src = os.path.join(CSRC, name + ".cpp")
         obj = os.path.join(OUT, name + ".o")

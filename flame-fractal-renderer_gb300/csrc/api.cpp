@@ -18,11 +18,7 @@
 #include "isaac64.cuh"
 #include "launch.h"
 
-using namespace ffr;
-
-namespace {
-
-thread_local std::string g_create_error = "no error";
+namespace ffr {
 
 // Isaac::init with flag = false (src/rng/isaac.hpp:93-131): randmem is the
 // golden-ratio constant mixed 4 times, then mixed once per 8 words.
@@ -49,6 +45,23 @@ void isaac_init_table(unsigned long long out[16])
         out[i + 4] = e; out[i + 5] = f; out[i + 6] = g; out[i + 7] = h;
     }
 }
+
+} // namespace ffr
+
+using namespace ffr;
+
+namespace {
+
+thread_local std::string g_create_error = "no error";
+
+} // namespace
+
+void ffr::set_global_error(const std::string& m)
+{
+    g_create_error = m;
+}
+
+namespace {
 
 typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
 typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);

@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "flame_program.h"
@@ -75,6 +76,12 @@ struct TraceArgs
     double* pts;                    // n * dims
     unsigned long long isaac_init[16];
 };
+
+// Isaac::init with flag = false: the 16-word randmem every stream starts from
+void isaac_init_table(unsigned long long out[16]);
+
+// set the message ffr_last_error(NULL) returns on this thread
+void set_global_error(const std::string& m);
 
 // the 16-word randmem table every stream starts from (isaac64.cuh)
 struct IsaacInit

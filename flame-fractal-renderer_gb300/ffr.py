@@ -38,7 +38,7 @@ EXPORTS = [
     "ffr_info", "ffr_size", "ffr_flame_json", "ffr_add_buffer", "ffr_render",
     "ffr_read_buffer", "ffr_load_buffer", "ffr_histogram", "ffr_clear",
     "ffr_isaac_words", "ffr_step", "ffr_trace", "ffr_plan",
-    "ffr_measure_atomic_rate",
+    "ffr_measure_atomic_rate", "ffr_render_noalloc",
 ]
 
 
@@ -111,6 +111,8 @@ def load_library(path: str = LIB_PATH):
         L.ffr_plan.argtypes = [vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         L.ffr_measure_atomic_rate.argtypes = [ctypes.c_int, u64, u64,
                                               ctypes.POINTER(ctypes.c_double)]
+        L.ffr_render_noalloc.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts), vp, vp,
+                                         u64, u64, u64, u64, ctypes.POINTER(Stats)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is ctypes.c_int:      # default: ffr_status

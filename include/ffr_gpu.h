@@ -191,6 +191,37 @@ ffr_status ffr_plan(ffr_ctx *ctx, uint64_t samples, uint64_t *streams,
 ffr_status ffr_measure_atomic_rate(int device, uint64_t cells, uint64_t ops,
                                    double *ops_per_s);
 
+/* ---------------------------------------------------------------------
+ * Render without device allocation.  No counterpart in the reference: the
+ * reference renders into a std::vector it allocates itself.
+ *
+ * For callers that cannot call cudaMalloc (their device memory belongs to
+ * another allocator -- a framework's caching pool, a fixed arena -- and a
+ * second allocator must not compete for it): they pass a count buffer they
+ * already own and the same render kernel as ffr_render accumulates into it.
+ * This call makes no device allocation (no cudaMalloc, cudaFree or
+ * allocating library routine); the flame JSON is parsed on the host as in
+ * ffr_create.
+ *
+ * d_counts: device array of `cells` u32 counts (the flame's buffer size,
+ *   x fastest), added to, never cleared.  Counts are 32-bit here: a cell must
+ *   have room for this call's hits; at most 2^32-1 samples per call.
+ * d_colors: device array of cells * color_dims f64 colour sums, required when
+ *   the flame has colour_dimensions > 0, else ignored.
+ * The kernel's scratch (flame program + statistics) is one fixed device
+ * array per GPU (about 180 KB, held until the process exits); flames whose
+ * program exceeds its 16 KB program part are rejected with FFR_ERR_ARG.
+ * The first call on a device looks up that array's device address (with
+ * that device current); make that first call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU (from several host
+ * threads) race, so serialise them.  Work runs on the legacy default stream
+ * and the call returns when it is done.  Errors: ffr_last_error(NULL).
+ * ------------------------------------------------------------------- */
+ffr_status ffr_render_noalloc(const char *json, size_t len, const ffr_opts *opts,
+                              uint32_t *d_counts, double *d_colors, uint64_t cells,
+                              uint64_t samples, uint64_t seed, uint64_t bad_limit,
+                              ffr_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif
