@@ -234,6 +234,7 @@ def main():
     t0 = time.perf_counter()
     kern_ms, binned, iters, launches = 0.0, 0, 0, 0
     streams = traj_len = 0
+    kernel_used = None
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -243,6 +244,7 @@ def main():
         iters += s.samples_iterated
         launches += 1
         streams, traj_len = s.streams, s.traj_len
+        kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel)
     barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
@@ -297,7 +299,7 @@ def main():
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "traffic": (dram_per_sample * binned / launches) if dram_per_sample else None,
                 "peak_source": peak_kind,
-                "kernel": "chaos_kernel<2,float> (render)"}
+                "kernel": f"render kernel ({kernel_used}), FP32"}
     atom = ffr.measure_atomic_rate(1920 * 1080, 1 << 31, device=local)
     l2 = {"peak_ops_per_s": atom, "achieved_ops_per_s": binned / (kern_ms * 1e-3),
           "frac": binned / (kern_ms * 1e-3) / atom,
@@ -306,7 +308,8 @@ def main():
     fp64 = None
     if not args.no_fp64:
         B64 = max(10**7, B // 10)
-        with ffr.BufferRenderer(text, precision=ffr.FP64, settle=settle, device=local) as r64:
+        with ffr.BufferRenderer(text, precision=ffr.FP64, settle=settle, device=local,
+                                kernel=ffr.KERNEL_PLAIN) as r64:
             r64.render(B64, 99)
             ms64, bin64 = 0.0, 0
             for k in range(3):
@@ -316,6 +319,7 @@ def main():
                 ms64 += s.kernel_ms
                 bin64 += s.samples_plotted - s.dropped
         fp64 = {"value": bin64 / (ms64 * 1e-3), "samples_per_step": B64,
+                "kernel": "plain FP64 mirror",
                 "fp32_over_fp64": value / ws / (bin64 / (ms64 * 1e-3))}
 
     cpu = None
@@ -334,6 +338,7 @@ def main():
         "data": "synthetic (seeded flame generator)",
         "config": {"workload": WORKLOAD, "samples_per_step": B, "settle": settle,
                    "seed": 7, "streams": streams, "traj_len": traj_len,
+                   "kernel": kernel_used,
                    "flush": "256 MiB L2 flush between timed steps",
                    "parallelism": f"replicas{ws}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": h2d,

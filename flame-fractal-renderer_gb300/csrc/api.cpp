@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <string>
@@ -67,25 +68,34 @@ typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
 typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
 typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
 typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
+typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
 
 struct Launchers
 {
     RenderFn render;
     OccFn occ;
+    RenderFn sorted;
+    OccSortedFn occ_sorted;
     StepFn step;
     TraceFn trace;
 };
 
 const Launchers kLaunchers[2][3] = {
     {
-        {launch_render_p0_d1, occupancy_p0_d1, launch_step_p0_d1, launch_trace_p0_d1},
-        {launch_render_p0_d2, occupancy_p0_d2, launch_step_p0_d2, launch_trace_p0_d2},
-        {launch_render_p0_d3, occupancy_p0_d3, launch_step_p0_d3, launch_trace_p0_d3},
+        {launch_render_p0_d1, occupancy_p0_d1, launch_sorted_p0_d1,
+         occupancy_sorted_p0_d1, launch_step_p0_d1, launch_trace_p0_d1},
+        {launch_render_p0_d2, occupancy_p0_d2, launch_sorted_p0_d2,
+         occupancy_sorted_p0_d2, launch_step_p0_d2, launch_trace_p0_d2},
+        {launch_render_p0_d3, occupancy_p0_d3, launch_sorted_p0_d3,
+         occupancy_sorted_p0_d3, launch_step_p0_d3, launch_trace_p0_d3},
     },
     {
-        {launch_render_p1_d1, occupancy_p1_d1, launch_step_p1_d1, launch_trace_p1_d1},
-        {launch_render_p1_d2, occupancy_p1_d2, launch_step_p1_d2, launch_trace_p1_d2},
-        {launch_render_p1_d3, occupancy_p1_d3, launch_step_p1_d3, launch_trace_p1_d3},
+        {launch_render_p1_d1, occupancy_p1_d1, launch_sorted_p1_d1,
+         occupancy_sorted_p1_d1, launch_step_p1_d1, launch_trace_p1_d1},
+        {launch_render_p1_d2, occupancy_p1_d2, launch_sorted_p1_d2,
+         occupancy_sorted_p1_d2, launch_step_p1_d2, launch_trace_p1_d2},
+        {launch_render_p1_d3, occupancy_p1_d3, launch_sorted_p1_d3,
+         occupancy_sorted_p1_d3, launch_step_p1_d3, launch_trace_p1_d3},
     },
 };
 
@@ -240,12 +250,39 @@ void destroy(ffr_ctx* c)
     delete c;
 }
 
-ffr_status plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* L, int* grid)
+static_assert(offsetof(ProgHeader<double>, rng_words_max)
+              == offsetof(ProgHeader<float>, rng_words_max), "program header layout");
+
+// words one selectable xform application draws at most (ProgHeader)
+int program_words(const ffr_ctx* c)
+{
+    const ProgHeader<double>* h = reinterpret_cast<const ProgHeader<double>*>(c->prog_host.data());
+    return (int)h->rng_words_max;       // same offset in the float header
+}
+
+ffr_status plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* L, int* grid,
+                int* kernel)
 {
     int bps = 0, block = 0;
     size_t smem = 0;
-    CU(c, c->L().occ(c->flame.color_dims > 0, c->d_hi != nullptr, &bps, &block,
-                     (unsigned int)c->prog_host.size(), (int)c->flame.xforms.size(), &smem));
+    const int color = c->flame.color_dims > 0, spill = c->d_hi != nullptr;
+    const unsigned int pb = (unsigned int)c->prog_host.size();
+    const int nxf = (int)c->flame.xforms.size();
+    int k = c->opts.kernel;
+    if (k != FFR_KERNEL_PLAIN)
+    {
+        CU(c, c->L().occ_sorted(color, spill, &bps, &block, pb, nxf, program_words(c), &smem));
+        if (bps >= 1)
+            k = FFR_KERNEL_SORTED;
+        else if (k == FFR_KERNEL_SORTED)
+            return fail(c, FFR_ERR_ARG, "xform-sorted kernel cannot run this flame (more than "
+                "16 xforms or not enough shared memory)");
+        else
+            k = FFR_KERNEL_PLAIN;
+    }
+    if (k == FFR_KERNEL_PLAIN)
+        CU(c, c->L().occ(color, spill, &bps, &block, pb, nxf, &smem));
+    *kernel = k;
     if (bps < 1)
         return fail(c, FFR_ERR_ARG, "render kernel does not fit on an SM "
             "(program " + std::to_string(c->prog_host.size()) + " bytes)");
@@ -289,6 +326,7 @@ void ffr_default_opts(ffr_opts* o)
     o->streams = 0;
     o->traj_len = 0;
     o->timeout_ms = 0;
+    o->kernel = FFR_KERNEL_AUTO;
 }
 
 ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ctx** out)
@@ -307,6 +345,8 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: ABI version mismatch");
     if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown precision");
+    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_SORTED)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown kernel");
     ffr_ctx* c = new (std::nothrow) ffr_ctx;
     if (!c)
         return fail(nullptr, FFR_ERR_OOM, "ffr_create: out of host memory");
@@ -486,8 +526,8 @@ ffr_status ffr_plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* t
         return FFR_ERR_ARG;
     CU(c, cudaSetDevice(c->device));
     uint64_t S = 0, L = 0;
-    int grid = 0;
-    ffr_status s = plan(c, samples, &S, &L, &grid);
+    int grid = 0, kernel = 0;
+    ffr_status s = plan(c, samples, &S, &L, &grid, &kernel);
     if (s != FFR_OK)
         return s;
     if (streams) *streams = S;
@@ -521,8 +561,8 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
             return s;
     }
     uint64_t S = 0, L = 0;
-    int grid = 0;
-    ffr_status s = plan(c, samples, &S, &L, &grid);
+    int grid = 0, kernel = 0;
+    ffr_status s = plan(c, samples, &S, &L, &grid, &kernel);
     if (s != FFR_OK)
         return s;
     // reset device stats: zero, then +inf / -inf extreme keys
@@ -555,10 +595,14 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     a.colors = c->d_colors;
     a.stats = c->d_stats;
     a.cancel = c->d_cancel;
+    a.rng_words = program_words(c);
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
     *c->h_cancel = 0u;
     CU(c, cudaEventRecord(c->ev0, c->stream));
-    CU(c, c->L().render(a, grid, c->stream));
+    if (kernel == FFR_KERNEL_SORTED)
+        CU(c, c->L().sorted(a, grid, c->stream));
+    else
+        CU(c, c->L().render(a, grid, c->stream));
     CU(c, cudaEventRecord(c->ev1, c->stream));
     s = wait_stream(c);
     c->count_bound += samples;
@@ -609,6 +653,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->streams = S;
         st->traj_len = L;
         st->kernel_ms = ms;
+        st->kernel = kernel;
     }
     const bool cancelled = hs->cancelled != 0;
     delete hs;

@@ -3,6 +3,7 @@
 // built with --fmad=false so no multiply-add is contracted: the reference
 // (and the oracle) round every product and sum separately.
 #include "chaos_kernel.cuh"
+#include "chaos_sorted.cuh"
 
 #if !defined(FFR_P) || !defined(FFR_D)
 #error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3>"
@@ -46,6 +47,63 @@ static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, size_t* s
         return e;
     *smem_out = smem;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kBlock, smem);
+}
+
+constexpr int kSortedBlock = 256;
+
+template <bool C, bool S>
+static cudaError_t launch_sorted_one(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    const size_t smem = sorted_smem_bytes<kSortedBlock>(
+        a.prog_bytes, a.nxf, a.rng_words, FFR_D, (int)sizeof(Real));
+    auto k = chaos_sorted_kernel<FFR_D, Real, C, S, kSortedBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, kSortedBlock, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool C, bool S>
+static cudaError_t occ_sorted_one(int* bps, unsigned int prog_bytes, int nxf, int words,
+                                  size_t* smem_out)
+{
+    const size_t smem = sorted_smem_bytes<kSortedBlock>(prog_bytes, nxf, words, FFR_D,
+                                                        (int)sizeof(Real));
+    auto k = chaos_sorted_kernel<FFR_D, Real, C, S, kSortedBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    *smem_out = smem;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kSortedBlock, smem);
+}
+
+cudaError_t FFR_NAME(launch_sorted)(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    if (a.color_dims > 0)
+        return a.spill ? launch_sorted_one<true, true>(a, grid, st)
+                       : launch_sorted_one<true, false>(a, grid, st);
+    return a.spill ? launch_sorted_one<false, true>(a, grid, st)
+                   : launch_sorted_one<false, false>(a, grid, st);
+}
+
+cudaError_t FFR_NAME(occupancy_sorted)(int color, int spill, int* blocks_per_sm, int* block,
+                                       unsigned int prog_bytes, int nxf, int words,
+                                       size_t* smem)
+{
+    *block = kSortedBlock;
+    if (nxf > kSortedMaxXforms)
+    {
+        *blocks_per_sm = 0;
+        return cudaSuccess;
+    }
+    if (color)
+        return spill ? occ_sorted_one<true, true>(blocks_per_sm, prog_bytes, nxf, words, smem)
+                     : occ_sorted_one<true, false>(blocks_per_sm, prog_bytes, nxf, words, smem);
+    return spill ? occ_sorted_one<false, true>(blocks_per_sm, prog_bytes, nxf, words, smem)
+                 : occ_sorted_one<false, false>(blocks_per_sm, prog_bytes, nxf, words, smem);
 }
 
 cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t st)

@@ -1,0 +1,441 @@
+// Xform-sorted ("wavefront") render kernel.
+//
+// Same per-stream semantics as chaos_body (chaos_kernel.cuh): stream s runs
+// its trajectories in order, drawing the reference's RNG words in the
+// reference's order (RenderIterator::_init / iterate,
+// src/renderers/render_iterator.hpp:52-139; BufferRenderer::_render_batch,
+// src/renderers/buffer_renderer.hpp:151-250), so FP64 buffers are identical
+// to the plain kernel's.  What changes is who evaluates each xform step:
+//
+//   phase A  (owner thread, one per stream)  draw the xform-choice word and
+//            the words that xform's variations will draw, stage the point,
+//            and enter the CTA's per-xform list with one __match_any_sync
+//            warp aggregation and one shared atomic per (warp, xform);
+//   phase B  (every warp)  take 32-entry chunks of one xform's list and apply
+//            that xform to the listed points: all lanes of a chunk run the
+//            same xform body, instead of a warp running the union of the
+//            xforms its lanes picked;
+//   phase C  (owner)  final xform, colour, statistics, bad values, binning.
+//
+// Two barriers per iteration; the list counters are double-buffered so the
+// next iteration's counters are zeroed during phase B.  A stream whose
+// trajectory hits a bad value re-settles through the same sorted path and
+// finishes the bad sample (extremes, stale final point binning) when its
+// settle iterations are done, as the reference does after iter.init().
+#pragma once
+
+#include "chaos_kernel.cuh"
+
+namespace ffr {
+
+// xforms a sorted CTA handles (per-xform lists and counters in shared memory)
+constexpr int kSortedMaxXforms = 16;
+
+template <int T>
+__host__ __device__ inline size_t sorted_smem_bytes(unsigned int prog_bytes, int nxf,
+                                                    int words, int dims, int real_bytes)
+{
+    size_t s = align16u(prog_bytes);
+    s += 2 * 16 * (size_t)T * 8;                          // ISAAC state
+    s += (size_t)words * T * 8;                           // pre-drawn words [W][T]
+    s += (((size_t)dims * T * real_bytes) + 15) & ~(size_t)15;   // staged points [D][T]
+    s += (((size_t)nxf * T * 4) + 15) & ~(size_t)15;      // per-thread xform counts
+    s += (((size_t)nxf * T * 2) + 15) & ~(size_t)15;      // per-xform lists (u16)
+    s += 2 * kSortedMaxXforms * 4;                        // list counters x2
+    return s;
+}
+
+// pre-drawn words of one owner, consumed in draw order by the worker
+template <int T>
+struct PreDrawn
+{
+    const uint64_t* w;
+    int k;
+    __device__ __forceinline__ uint64_t next() { return w[(k++) * T]; }
+};
+
+template <int D, typename R, bool COLOR, bool SPILL, int T>
+__device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* smem)
+{
+    using Tr = RealTraits<R>;
+    Prog<R> pg;
+    pg.bind(smem);
+    const ProgHeader<R>& h = *pg.h;
+    const int nxf = a.nxf;
+    const int W = (int)h.rng_words_max;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    constexpr int kWarps = T / 32;
+
+    unsigned char* q = smem + align16u(a.prog_bytes);
+    uint64_t* imem = reinterpret_cast<uint64_t*>(q);
+    q += 16 * T * 8;
+    uint64_t* irsl = reinterpret_cast<uint64_t*>(q);
+    q += 16 * T * 8;
+    uint64_t* words = reinterpret_cast<uint64_t*>(q);
+    q += (size_t)W * T * 8;
+    R* stage = reinterpret_cast<R*>(q);
+    q += ((size_t)D * T * sizeof(R) + 15) & ~(size_t)15;
+    uint32_t* xfc = reinterpret_cast<uint32_t*>(q);
+    q += ((size_t)nxf * T * 4 + 15) & ~(size_t)15;
+    uint16_t* list = reinterpret_cast<uint16_t*>(q);
+    q += ((size_t)nxf * T * 2 + 15) & ~(size_t)15;
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(q);         // [2][kSortedMaxXforms]
+
+    for (int i = 0; i < nxf; ++i)
+        xfc[i * T + tid] = 0u;
+    if (tid < 2 * kSortedMaxXforms)
+        cnt[tid] = 0u;
+
+    DevIsaac<T> rng;
+    rng.mem = imem + tid;
+    rng.rsl = irsl + tid;
+
+    unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
+    R ext_lo[D], ext_hi[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+    {
+        ext_lo[i] = R(1) / R(0);
+        ext_hi[i] = -R(1) / R(0);
+    }
+    const int r = COLOR ? a.color_dims : 0;
+    R c[COLOR ? kMaxColorDims : 1], cf[COLOR ? kMaxColorDims : 1];
+    (void)c; (void)cf;
+
+    const unsigned long long L = a.traj_len;
+    const unsigned long long ntraj = (a.samples + L - 1) / L;
+    const unsigned long long nstreams = a.streams < ntraj ? a.streams : ntraj;
+    const unsigned long long gstride = (unsigned long long)gridDim.x * T;
+    volatile unsigned int* vstop = &a.stats->stop;
+
+    // owner state
+    unsigned long long s = (unsigned long long)blockIdx.x * T + tid;
+    unsigned long long tj = s;
+    unsigned long long len = 0;
+    unsigned long long settle_left = 0;
+    bool pending = false;          // bad sample waiting for its re-settle
+    bool active = false;
+    R p[D], pf[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        p[i] = pf[i] = R(0);
+    unsigned int poll = 0;
+
+    auto colour_init = [&]() {
+        if (COLOR)
+            for (int i = 0; i < r; ++i)
+                c[i] = Tr::unit(rng.next());
+    };
+    // RenderIterator::_init up to the settle loop (render_iterator.hpp:54)
+    auto start_point = [&]() {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            p[i] = R(2) * Tr::unit(rng.next()) - R(1);
+        settle_left = a.settle;
+        if (settle_left == 0)
+            colour_init();
+    };
+    // next trajectory of this stream, or of the next stream of this thread
+    auto next_trajectory = [&](bool first) -> bool {
+        if (!first)
+            tj += a.streams;
+        for (;;)
+        {
+            if (s >= nstreams)
+                return false;
+            if (tj < ntraj)
+                break;
+            s += gstride;
+            tj = s;
+            first = true;
+        }
+        if (first && tj == s)
+            rng.seed(stream_key(a.seed, s), a.isaac_init);
+        if (*vstop)
+            return false;
+        len = a.samples - tj * L;
+        if (len > L)
+            len = L;
+        start_point();
+        return true;
+    };
+    // extremes, bounds, index and binning of a finished sample
+    auto tail = [&]() {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
+            ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
+        }
+        bool inb = true;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            inb &= (pf[i] >= h.lo[i]) && (pf[i] <= h.hi[i]);
+        if (!inb)
+            return;
+        ++s_plot;
+        uint64_t bi;
+        if (sizeof(R) == sizeof(double))
+        {
+            bi = to_index<R>((pf[0] - h.lo[0]) * h.mult_d[0]);
+#pragma unroll
+            for (int i = 1; i < D; ++i)
+                bi += to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]) * h.mult_i[i];
+        }
+        else
+        {
+            bi = 0;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+            {
+                uint64_t di = to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]);
+                di = di < h.size[i] ? di : h.size[i] - 1;
+                bi += di * h.mult_i[i];
+            }
+        }
+        if (bi >= h.cells)
+        {
+            ++dropped;
+            return;
+        }
+        if (SPILL)
+        {
+            const unsigned int old = atomicAdd(&a.counts[bi], 1u);
+            if (old == 0xFFFFFFFFu)
+                atomicAdd(&a.hi[bi], 1u);
+        }
+        else
+            atomicAdd(&a.counts[bi], 1u);
+        if (COLOR)
+            for (int i = 0; i < r; ++i)
+                atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));
+    };
+    auto sample_done = [&]() {
+        if (--len == 0)
+            active = next_trajectory(false);
+    };
+
+    __syncthreads();
+    active = next_trajectory(true);
+    int parity = 0;
+    for (;;)
+    {
+        // ---- phase A: choose, pre-draw, stage, list
+        int x = -1;
+        if (active)
+        {
+            x = pick_xform<R>(pg, rng);
+            const int nw = pg.xf[x].rng_words;
+            for (int j = 0; j < nw; ++j)
+                words[j * T + tid] = rng.next();
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                stage[i * T + tid] = p[i];
+        }
+        uint32_t* cc = cnt + parity * kSortedMaxXforms;
+        const unsigned int same = __match_any_sync(0xffffffffu, x);
+        const int leader = __ffs(same) - 1;
+        unsigned int base = 0;
+        if (lane == leader && x >= 0)
+            base = atomicAdd(&cc[x], (unsigned int)__popc(same));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (x >= 0)
+            list[x * T + base + __popc(same & ((1u << lane) - 1u))] = (uint16_t)tid;
+        if (!__syncthreads_or(active))
+            break;
+
+        // ---- phase B: uniform-xform chunks
+        if (tid < kSortedMaxXforms)
+            cnt[(parity ^ 1) * kSortedMaxXforms + tid] = 0u;
+        int total = 0;
+        for (int i = 0; i < nxf; ++i)
+            total += (int)((cc[i] + 31u) >> 5);
+        for (int ch = warp; ch < total; ch += kWarps)
+        {
+            int i = 0, acc = 0;
+            for (;;)
+            {
+                const int n = (int)((cc[i] + 31u) >> 5);
+                if (ch < acc + n)
+                    break;
+                acc += n;
+                ++i;
+            }
+            const unsigned int k = (unsigned int)(ch - acc) * 32u + lane;
+            if (k < cc[i])
+            {
+                const int o = list[i * T + k];
+                R pin[D], pout[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    pin[d] = stage[d * T + o];
+                PreDrawn<T> pw{words + o, 0};
+                apply_xform<D, R>(pg, pg.xf[i], pin, pout, pw);
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    stage[d * T + o] = pout[d];
+            }
+        }
+        __syncthreads();
+        parity ^= 1;
+
+        // ---- phase C: owner finishes its sample
+        if (!active)
+            continue;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            p[i] = stage[i * T + tid];
+        if (settle_left > 0)
+        {
+            // settle iteration (render_iterator.hpp:55-56): no final xform,
+            // no colour, no statistics
+            if (--settle_left == 0)
+            {
+                colour_init();
+                if (pending)
+                {
+                    pending = false;
+                    tail();
+                    sample_done();
+                }
+            }
+        }
+        else
+        {
+            const XformT<R>& xf = pg.xf[x];
+            if (COLOR && xf.has_color)
+            {
+                const R sp = xf.color_speed;
+                const R* col = pg.color + (size_t)x * r;
+                for (int i = 0; i < r; ++i)
+                    c[i] = (R(1) - sp) * c[i] + sp * col[i];
+            }
+            if (h.has_final)
+            {
+                const XformT<R>& ff = pg.xf[nxf];
+                apply_xform<D, R>(pg, ff, p, pf, rng);
+                if (COLOR)
+                {
+                    if (ff.has_color)
+                    {
+                        const R sp = ff.color_speed;
+                        const R* col = pg.color + (size_t)nxf * r;
+                        for (int i = 0; i < r; ++i)
+                            cf[i] = (R(1) - sp) * c[i] + sp * col[i];
+                    }
+                    else
+                        for (int i = 0; i < r; ++i)
+                            cf[i] = c[i];
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int i = 0; i < D; ++i)
+                    pf[i] = p[i];
+                if (COLOR)
+                    for (int i = 0; i < r; ++i)
+                        cf[i] = c[i];
+            }
+            ++s_iter;
+            ++xfc[x * T + tid];
+            if (bad_point<D, R>(p))
+            {
+                const unsigned long long tot = atomicAdd(&a.stats->bad_total, 1ull) + 1;
+                const unsigned long long slot = atomicAdd(&a.stats->bad_claim, 1ull);
+                if (slot < (unsigned long long)kMaxBadRecords)
+                {
+                    a.stats->bad_xf[slot] = xf.id;
+#pragma unroll
+                    for (int i = 0; i < D; ++i)
+                        a.stats->bad_pts[slot][i] = as_double(p[i]);
+                }
+                if (tot > a.bad_limit)
+                {
+                    atomicExch(&a.stats->stop, 1u);
+                    active = false;
+                    continue;
+                }
+                // iter.init(): new start, re-settle, then finish this sample
+                start_point();
+                if (settle_left == 0)
+                {
+                    tail();
+                    sample_done();
+                }
+                else
+                    pending = true;
+            }
+            else
+            {
+                tail();
+                sample_done();
+            }
+        }
+        if (active && ((++poll) & kStopPollMask) == 0)
+        {
+            if (*vstop || (a.cancel && *a.cancel))
+            {
+                if (a.cancel && *a.cancel)
+                    atomicExch(&a.stats->cancelled, 1u);
+                active = false;
+            }
+        }
+    }
+
+    // statistics: warp reduce, one atomic per warp
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        s_iter += __shfl_down_sync(0xffffffffu, s_iter, off);
+        s_plot += __shfl_down_sync(0xffffffffu, s_plot, off);
+        dropped += __shfl_down_sync(0xffffffffu, dropped, off);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            const R lo = __shfl_down_sync(0xffffffffu, ext_lo[i], off);
+            const R hi = __shfl_down_sync(0xffffffffu, ext_hi[i], off);
+            ext_lo[i] = lo < ext_lo[i] ? lo : ext_lo[i];
+            ext_hi[i] = hi > ext_hi[i] ? hi : ext_hi[i];
+        }
+    }
+    if (lane == 0)
+    {
+        if (s_iter)
+            atomicAdd(&a.stats->s_iter, s_iter);
+        if (s_plot)
+            atomicAdd(&a.stats->s_plot, s_plot);
+        if (dropped)
+            atomicAdd(&a.stats->dropped, dropped);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            if (ext_lo[i] == ext_lo[i] && ext_lo[i] != R(1) / R(0))
+                atomicMin(&a.stats->ext_lo[i], order_key(as_double(ext_lo[i])));
+            if (ext_hi[i] == ext_hi[i] && ext_hi[i] != -R(1) / R(0))
+                atomicMax(&a.stats->ext_hi[i], order_key(as_double(ext_hi[i])));
+        }
+    }
+    for (int i = 0; i < nxf; ++i)
+    {
+        unsigned long long v = xfc[i * T + tid];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0 && v)
+            atomicAdd(&a.stats->xf_dist[i], v);
+    }
+}
+
+template <int D, typename R, bool COLOR, bool SPILL, int T>
+__global__ void __launch_bounds__(T) chaos_sorted_kernel(const RenderArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    load_program<T>(smem, a.prog, a.prog_bytes);
+    __syncthreads();
+    sorted_body<D, R, COLOR, SPILL, T>(a, smem);
+}
+
+} // namespace ffr

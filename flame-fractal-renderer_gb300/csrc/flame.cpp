@@ -302,6 +302,10 @@ void pack_xform(const HostXform& h, int dims, XformT<R>& x, int16_t var_begin)
     x.has_pre = h.has_pre;
     x.has_post = h.has_post;
     x.has_color = !h.color.empty();
+    uint32_t w = 0;
+    for (const auto& v : h.vars)
+        w += v.rng_words;
+    x.rng_words = (uint8_t)std::min<uint32_t>(w, 255);
 }
 
 } // namespace
@@ -340,16 +344,18 @@ std::vector<uint8_t> build_program(const HostFlame& f)
             + std::to_string(off) + " bytes; limit "
             + std::to_string(kMaxProgramBytes) + ")");
     h.total_bytes = (uint32_t)off;
+    // the largest draw count of one selectable xform application (the final
+    // xform is applied by the stream's owner thread and draws directly)
     uint32_t words = 0;
-    for (const HostXform* x : all)
+    for (int k = 0; k < nxf; ++k)
     {
-        if (!x)
-            continue;
         uint32_t w = 0;
-        for (const auto& v : x->vars)
+        for (const auto& v : all[k]->vars)
             w += v.rng_words;
         words = std::max(words, w);
     }
+    if (words > 255)
+        throw FlameError("an xform draws more than 255 random words per application");
     h.rng_words_max = words;
     for (int i = 0; i < f.dims; ++i)
     {

@@ -47,7 +47,7 @@ struct alignas(16) XformT
     uint8_t has_pre;
     uint8_t has_post;
     uint8_t has_color;
-    uint8_t pad;
+    uint8_t rng_words;      // RNG words one application draws (fixed per xform)
 };
 
 template <typename R>

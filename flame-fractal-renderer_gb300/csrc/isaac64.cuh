@@ -51,27 +51,30 @@ struct DevIsaac
     __device__ __forceinline__ uint64_t& M(int i) { return mem[i * BLOCK]; }
     __device__ __forceinline__ uint64_t& Rs(int i) { return rsl[i * BLOCK]; }
 
-    __device__ __noinline__ void gen()
+    // one rngstep (isaac.hpp:146-153) at state index i with mixed a value mx
+    __device__ __forceinline__ void step(int i, uint64_t mx, uint64_t& aa, uint64_t& bb)
+    {
+        const uint64_t x = M(i);
+        aa = mx + M((i + 8) & 15);
+        const uint64_t y = M((int)((x >> 3) & 15)) + aa + bb;
+        M(i) = y;
+        bb = M((int)((y >> 7) & 15)) + x;
+        Rs(i) = bb;
+    }
+
+    // Isaac::gen: 16 rngsteps in four rngstep4 groups; kept as a rolled
+    // loop so each inlined copy is small and no call ABI is involved
+    __device__ __forceinline__ void gen()
     {
         uint64_t aa = a;
         uint64_t bb = b + (++c);
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
+#pragma unroll 1
+        for (int i = 0; i < 16; i += 4)
         {
-            const uint64_t x = M(i);
-            uint64_t mx;
-            switch (i & 3)
-            {
-            case 0: mx = ~(aa ^ (aa << 21)); break;
-            case 1: mx = aa ^ (aa >> 5); break;
-            case 2: mx = aa ^ (aa << 12); break;
-            default: mx = aa ^ (aa >> 33); break;
-            }
-            aa = mx + M((i + 8) & 15);
-            const uint64_t y = M((int)((x >> 3) & 15)) + aa + bb;
-            M(i) = y;
-            bb = M((int)((y >> 7) & 15)) + x;
-            Rs(i) = bb;
+            step(i + 0, ~(aa ^ (aa << 21)), aa, bb);
+            step(i + 1, aa ^ (aa >> 5), aa, bb);
+            step(i + 2, aa ^ (aa << 12), aa, bb);
+            step(i + 3, aa ^ (aa >> 33), aa, bb);
         }
         a = aa;
         b = bb;

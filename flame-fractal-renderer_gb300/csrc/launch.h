@@ -48,6 +48,7 @@ struct RenderArgs
     double* colors;                 // cells * color_dims, or null
     DevStats* stats;
     const volatile unsigned int* cancel;   // host-mapped cancel flag, or null
+    int rng_words;                  // largest RNG draw of one xform (sorted kernel)
     unsigned long long isaac_init[16];
 };
 
@@ -96,6 +97,12 @@ struct IsaacInit
     cudaError_t occupancy_p##P##_d##D(int color, int spill, int* blocks_per_sm, \
                                       int* block, unsigned int prog_bytes,      \
                                       int nxf, size_t* smem);                   \
+    cudaError_t launch_sorted_p##P##_d##D(const RenderArgs&, int grid,          \
+                                          cudaStream_t);                        \
+    cudaError_t occupancy_sorted_p##P##_d##D(int color, int spill,              \
+                                             int* blocks_per_sm, int* block,    \
+                                             unsigned int prog_bytes, int nxf,  \
+                                             int words, size_t* smem);          \
     cudaError_t launch_step_p##P##_d##D(const StepArgs&, cudaStream_t);         \
     cudaError_t launch_trace_p##P##_d##D(const TraceArgs&, cudaStream_t);
 

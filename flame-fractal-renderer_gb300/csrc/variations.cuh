@@ -36,6 +36,7 @@ template <> struct RealTraits<double>
     __device__ static __forceinline__ double atan2_(double y, double x) { return atan2(y, x); }
     __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
     __device__ static __forceinline__ double fabs_(double x) { return fabs(x); }
+    __device__ static __forceinline__ double recip_(double x) { return 1.0 / x; }
 };
 
 template <> struct RealTraits<float>
@@ -50,12 +51,15 @@ template <> struct RealTraits<float>
     {
         return (float)(uint32_t)(w >> 40) * 0x1p-24f;
     }
-    __device__ static __forceinline__ float sin_(float x) { return sinf(x); }
-    __device__ static __forceinline__ float cos_(float x) { return cosf(x); }
-    __device__ static __forceinline__ void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+    // FP32 mode: SFU approximations (sin, cos, reciprocal); accepted by the
+    // histogram total-variation check against the FP64 oracle
+    __device__ static __forceinline__ float sin_(float x) { return __sinf(x); }
+    __device__ static __forceinline__ float cos_(float x) { return __cosf(x); }
+    __device__ static __forceinline__ void sincos_(float x, float* s, float* c) { __sincosf(x, s, c); }
     __device__ static __forceinline__ float atan2_(float y, float x) { return atan2f(y, x); }
     __device__ static __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     __device__ static __forceinline__ float fabs_(float x) { return fabsf(x); }
+    __device__ static __forceinline__ float recip_(float x) { return __fdividef(1.0f, x); }
 };
 
 // t[i] for a run-time i without dynamic register indexing
@@ -96,7 +100,7 @@ __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rn
 #pragma unroll
         for (int i = 1; i < D; ++i)
             r2 += t[i] * t[i];
-        const R r = R(1) / (r2 + T::eps);
+        const R r = T::recip_(r2 + T::eps);
 #pragma unroll
         for (int i = 0; i < D; ++i)
             o[i] = t[i] * r;
@@ -115,7 +119,7 @@ __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rn
     case V_HORSESHOE:                    // variations.hpp:527-540
     {
         const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-        const R r = R(1) / (T::sqrt_(x * x + y * y) + T::eps);
+        const R r = T::recip_(T::sqrt_(x * x + y * y) + T::eps);
         x2 = ((x - y) * (x + y)) * r;
         y2 = (R(2) * x * y) * r;
         break;

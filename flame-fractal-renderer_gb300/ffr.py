@@ -31,6 +31,7 @@ STATUS_NAMES = ["FFR_OK", "FFR_BAD_VALUES", "FFR_ERR_PARSE", "FFR_ERR_ARG",
                 "FFR_ERR_IO", "FFR_ERR_OOM", "FFR_ERR_TIMEOUT", "FFR_ERR_CUDA",
                 "FFR_ERR_STATE"]
 FP64, FP32 = 0, 1
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED = 0, 1, 2
 
 # every symbol include/ffr_gpu.h declares
 EXPORTS = [
@@ -51,7 +52,7 @@ class FfrError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("abi_version", ctypes.c_uint32), ("device", ctypes.c_int32),
-                ("precision", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("kernel", ctypes.c_int32),
                 ("settle", ctypes.c_uint64), ("streams", ctypes.c_uint64),
                 ("traj_len", ctypes.c_uint64), ("timeout_ms", ctypes.c_uint64)]
 
@@ -68,7 +69,8 @@ class Stats(ctypes.Structure):
                 ("bad_xf", ctypes.c_uint64 * MAX_BAD_RECORDS),
                 ("bad_pts", (ctypes.c_double * MAX_DIMS) * MAX_BAD_RECORDS),
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
-                ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double)]
+                ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
+                ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 _lib = None
@@ -148,6 +150,7 @@ class RenderStats:
     traj_len: int
     settle: int
     kernel_ms: float
+    kernel: int
 
     @property
     def ok(self) -> bool:
@@ -175,7 +178,7 @@ class BufferRenderer:
 
     def __init__(self, flame, precision: int = FP64, settle: int = 53,
                  streams: int = 0, traj_len: int = 0, device: int = 0,
-                 timeout_ms: int = 0):
+                 timeout_ms: int = 0, kernel: int = KERNEL_AUTO):
         self._lib = load_library()
         text = flame if isinstance(flame, str) else json.dumps(flame)
         raw = text.encode("utf-8")
@@ -183,6 +186,7 @@ class BufferRenderer:
         self._lib.ffr_default_opts(ctypes.byref(o))
         o.device, o.precision, o.settle = device, precision, settle
         o.streams, o.traj_len, o.timeout_ms = streams, traj_len, timeout_ms
+        o.kernel = kernel
         ctx = ctypes.c_void_p()
         st = self._lib.ffr_create(raw, len(raw), ctypes.byref(o), ctypes.byref(ctx))
         if st != FFR_OK:
@@ -244,7 +248,7 @@ class BufferRenderer:
             bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
             bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
             streams=st.streams, traj_len=st.traj_len, settle=st.settle,
-            kernel_ms=st.kernel_ms)
+            kernel_ms=st.kernel_ms, kernel=st.kernel)
 
     def plan(self, samples: int):
         s, L = ctypes.c_uint64(), ctypes.c_uint64()

@@ -59,7 +59,10 @@ typedef struct ffr_opts {
     uint32_t abi_version;      /* FFR_ABI_VERSION */
     int32_t device;            /* CUDA device ordinal */
     int32_t precision;         /* ffr_precision */
-    int32_t reserved0;
+    /* render kernel: 0 = automatic, 1 = plain (one thread runs its
+       trajectory's xforms, lanes diverge), 2 = xform-sorted (a CTA groups
+       its threads' points by chosen xform each step); same results */
+    int32_t kernel;
     /* iterations discarded at each trajectory start; the reference uses
        settle_iters<double> = 53 (src/types/constants.hpp:41-47) */
     uint64_t settle;
@@ -76,6 +79,8 @@ typedef struct ffr_opts {
 #define FFR_MAX_DIMS 3
 #define FFR_MAX_XFORM_IDS 4096
 #define FFR_MAX_BAD_RECORDS 4096
+
+enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2 };
 
 typedef struct ffr_stats {
     uint64_t samples_iterated;   /* getSamplesIterated */
@@ -95,6 +100,8 @@ typedef struct ffr_stats {
     uint64_t traj_len;
     uint64_t settle;
     double kernel_ms;            /* device time of the render kernel(s) */
+    int32_t kernel;              /* FFR_KERNEL_PLAIN or FFR_KERNEL_SORTED */
+    int32_t reserved;
 } ffr_stats;
 
 typedef struct ffr_ctx ffr_ctx;

@@ -111,15 +111,20 @@ def test_trace_fp32_choices_exact(ffr, name):
     np.testing.assert_array_equal(ids, d["trace_ids"])
 
 
+KERNELS = [1, 2]      # FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED
+
+
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
 @pytest.mark.parametrize("case", MAN["renders"], ids=lambda c: f"{c['key']}-{c['flame']}")
-def test_render_fp64_matches_reference(ffr, case):
+def test_render_fp64_matches_reference(ffr, case, kernel):
     d = npz(case["key"])
     st = case["stats"]
     with ffr.BufferRenderer(golden_flame_text(case["flame"]), precision=ffr.FP64,
                             settle=case["settle"], streams=case["streams"],
-                            traj_len=case["traj_len"]) as r:
+                            traj_len=case["traj_len"], kernel=kernel) as r:
         s = r.render(case["samples"], case["seed"], case["bad_limit"])
         buf = r.buffer_array()
+    assert s.kernel == kernel
     counts = buf[:, 0]
     assert s.ok == bool(st["ok"])
     assert s.samples_iterated == st["s_iter"]
@@ -139,14 +144,16 @@ def test_render_fp64_matches_reference(ffr, case):
         assert tv(counts, d["counts"]) < 0.2
 
 
-def test_render_large_exact_vs_oracle(ffr, fo, flames):
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
+def test_render_large_exact_vs_oracle(ffr, fo, flames, kernel):
     """1024^2 Sierpinski, 10^7 samples over 10^4 streams: bit-exact buffer."""
     fl = flames.sierpinski_2d(size=(1024, 1024))
     text = json.dumps(fl)
     of = fo.OracleFlame(fo.load_flame(text))
     seed, S, N, L, Z = 1, 10_000, 10_000_000, 1000, 20
     ref = fo.render(of, seed, S, N, L, Z, threads=8)
-    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L) as r:
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L,
+                            kernel=kernel) as r:
         s = r.render(N, seed)
         got = r.counts()
     np.testing.assert_array_equal(got, ref.counts)
@@ -154,13 +161,15 @@ def test_render_large_exact_vs_oracle(ffr, fo, flames):
     assert s.xf_dist.tolist() == ref.xf_dist.tolist()
 
 
-def test_render_3d_exact_vs_oracle(ffr, fo, flames):
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
+def test_render_3d_exact_vs_oracle(ffr, fo, flames, kernel):
     fl = flames.tetrahedron_3d(size=(128, 128, 128))
     text = json.dumps(fl)
     of = fo.OracleFlame(fo.load_flame(text))
     seed, S, N, L, Z = 3, 4096, 4_000_000, 977, 20
     ref = fo.render(of, seed, S, N, L, Z, threads=8)
-    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L) as r:
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=Z, streams=S, traj_len=L,
+                            kernel=kernel) as r:
         r.render(N, seed)
         got = r.counts()
     np.testing.assert_array_equal(got, ref.counts)
@@ -207,9 +216,10 @@ def test_counts_past_2_pow_32(ffr, fo, flames):
     assert got.max() > (1 << 32)
 
 
-def test_bad_value_limit_stops(ffr):
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
+def test_bad_value_limit_stops(ffr, kernel):
     text = golden_flame_text("badval")
-    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=10_000) as r:
+    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=10_000, kernel=kernel) as r:
         s = r.render(640_000, 3, bad_limit=5)
         assert s.status == ffr.FFR_BAD_VALUES
         assert s.bad_values > 5
@@ -219,10 +229,11 @@ def test_bad_value_limit_stops(ffr):
         assert s.samples_iterated < 640_000
 
 
-def test_bad_values_recorded_without_stop(ffr, fo):
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
+def test_bad_values_recorded_without_stop(ffr, fo, kernel):
     text = golden_flame_text("badval")
     of = fo.OracleFlame(fo.load_flame(text))
-    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=1000) as r:
+    with ffr.BufferRenderer(text, settle=20, streams=64, traj_len=1000, kernel=kernel) as r:
         s = r.render(64_000, 4, bad_limit=10**9)
         got = r.counts()
     ref = fo.render(of, 4, 64, 64_000, 1000, 20, bad_limit=10**9)
@@ -233,9 +244,11 @@ def test_bad_values_recorded_without_stop(ffr, fo):
     assert set(s.bad_xf.tolist()) <= {0, 1}
 
 
-def test_timeout_cancels_and_context_survives(ffr, flames):
+@pytest.mark.parametrize("kernel", KERNELS, ids=["plain", "sorted"])
+def test_timeout_cancels_and_context_survives(ffr, flames, kernel):
     text = json.dumps(flames.random_2d(7))
-    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=20, timeout_ms=30) as r:
+    with ffr.BufferRenderer(text, precision=ffr.FP64, settle=20, timeout_ms=30,
+                            kernel=kernel) as r:
         with pytest.raises(ffr.FfrError) as e:
             r.render(50_000_000_000, 1)
         assert e.value.status == ffr.FFR_ERR_TIMEOUT
