@@ -5,23 +5,31 @@
 // reference's order (RenderIterator::_init / iterate,
 // src/renderers/render_iterator.hpp:52-139; BufferRenderer::_render_batch,
 // src/renderers/buffer_renderer.hpp:151-250), so FP64 buffers are identical
-// to the plain kernel's.  What changes is who evaluates each xform step:
+// to the plain kernel's.  What changes is who does which part of a step:
 //
 //   phase A  (owner thread, one per stream)  draw the xform-choice word and
 //            the words that xform's variations will draw, stage the point,
-//            and enter the CTA's per-xform list with one __match_any_sync
-//            warp aggregation and one shared atomic per (warp, xform);
-//   phase B  (every warp)  take 32-entry chunks of one xform's list and apply
-//            that xform to the listed points: all lanes of a chunk run the
-//            same xform body, instead of a warp running the union of the
-//            xforms its lanes picked;
+//            enter the CTA's per-xform list (one __match_any_sync warp
+//            aggregation + one shared atomic per (warp, xform)), and when
+//            fewer than `low` words are left, queue an ISAAC refill;
+//   phase B  (every warp)  first the queued refills, 32 streams per warp at
+//            a time, then 32-entry chunks of one xform's list: every lane of
+//            a chunk runs the same xform body, instead of a warp running the
+//            union of the xforms (and refills) its lanes happen to need;
 //   phase C  (owner)  final xform, colour, statistics, bad values, binning.
 //
-// Two barriers per iteration; the list counters are double-buffered so the
-// next iteration's counters are zeroed during phase B.  A stream whose
-// trajectory hits a bad value re-settles through the same sorted path and
-// finishes the bad sample (extremes, stale final point binning) when its
-// settle iterations are done, as the reference does after iter.init().
+// ISAAC state of each stream lives in shared memory as [word][thread]:
+// randmem (16 words), randa/b/c, and a 24-word result array.  Words are
+// consumed from rsl[cnt-1] downwards (Isaac::next, src/rng/isaac.hpp:
+// 321-329).  A refill moves the cnt unconsumed words up to rsl[16..16+cnt)
+// and generates the next 16 into rsl[0..16), so consumption simply continues
+// downwards: the word sequence is the reference's, only its timing moves.
+//
+// Two barriers per iteration; list counters are double-buffered and the next
+// iteration's are zeroed during phase B.  A stream whose trajectory hits a
+// bad value re-settles through the same sorted path and finishes the bad
+// sample (extremes, stale final point) when its settle iterations are done,
+// as the reference does after iter.init().
 #pragma once
 
 #include "chaos_kernel.cuh"
@@ -30,20 +38,103 @@ namespace ffr {
 
 // xforms a sorted CTA handles (per-xform lists and counters in shared memory)
 constexpr int kSortedMaxXforms = 16;
+constexpr int kRslWords = 24;          // 16 fresh words + carried tail
+constexpr int kMaxRefillLow = kRslWords - 16;
 
 template <int T>
 __host__ __device__ inline size_t sorted_smem_bytes(unsigned int prog_bytes, int nxf,
                                                     int words, int dims, int real_bytes)
 {
     size_t s = align16u(prog_bytes);
-    s += 2 * 16 * (size_t)T * 8;                          // ISAAC state
+    s += (16 + kRslWords + 3) * (size_t)T * 8;            // ISAAC state
     s += (size_t)words * T * 8;                           // pre-drawn words [W][T]
     s += (((size_t)dims * T * real_bytes) + 15) & ~(size_t)15;   // staged points [D][T]
     s += (((size_t)nxf * T * 4) + 15) & ~(size_t)15;      // per-thread xform counts
     s += (((size_t)nxf * T * 2) + 15) & ~(size_t)15;      // per-xform lists (u16)
-    s += 2 * kSortedMaxXforms * 4;                        // list counters x2
+    s += (((size_t)T * 2) + 15) & ~(size_t)15;            // refill list (u16)
+    s += (((size_t)T) + 15) & ~(size_t)15;                // words left at refill (u8)
+    s += (2 * kSortedMaxXforms + 2) * 4;                  // list counters x2
     return s;
 }
+
+// ISAAC state of one stream in shared memory, stride T
+template <int T>
+struct SmemIsaac
+{
+    uint64_t* mem;      // [16]
+    uint64_t* rsl;      // [kRslWords]
+    uint64_t* abc;      // [3]: randa, randb, randc
+
+    __device__ __forceinline__ uint64_t& M(int i) { return mem[i * T]; }
+
+    __device__ __forceinline__ void step(int i, uint64_t mx, uint64_t& aa, uint64_t& bb)
+    {
+        const uint64_t x = M(i);
+        aa = mx + M((i + 8) & 15);
+        const uint64_t y = M((int)((x >> 3) & 15)) + aa + bb;
+        M(i) = y;
+        bb = M((int)((y >> 7) & 15)) + x;
+        rsl[i * T] = bb;
+    }
+
+    // Isaac::gen (isaac.hpp:77-90) into rsl[0..16)
+    __device__ __forceinline__ void gen()
+    {
+        uint64_t aa = abc[0];
+        const uint64_t cc = abc[2 * T] + 1;
+        uint64_t bb = abc[T] + cc;
+#pragma unroll 1
+        for (int i = 0; i < 16; i += 4)
+        {
+            step(i + 0, ~(aa ^ (aa << 21)), aa, bb);
+            step(i + 1, aa ^ (aa >> 5), aa, bb);
+            step(i + 2, aa ^ (aa << 12), aa, bb);
+            step(i + 3, aa ^ (aa >> 33), aa, bb);
+        }
+        abc[0] = aa;
+        abc[T] = bb;
+        abc[2 * T] = cc;
+    }
+
+    // keep the `left` unconsumed words (rsl[0..left)) above the new block
+    __device__ __forceinline__ void refill(int left)
+    {
+        for (int k = left - 1; k >= 0; --k)
+            rsl[(16 + k) * T] = rsl[k * T];
+        gen();
+    }
+
+    template <typename W>
+    __device__ __forceinline__ void seed(uint64_t key, const W* init16)
+    {
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+            M(i) = init16[i];
+        abc[0] = key;
+        abc[T] = ~key;
+        abc[2 * T] = key ^ kIsaacSeedXor;
+        gen();
+    }
+};
+
+// the owner's view: Isaac::next over the shared state
+template <int T>
+struct OwnerRng
+{
+    SmemIsaac<T> st;
+    int cnt;
+    __device__ __forceinline__ uint64_t next()
+    {
+        if (cnt == 0)
+        {
+            // rare: more words than the queued refills provided
+            st.gen();
+            cnt = 16;
+        }
+        --cnt;
+        return st.rsl[cnt * T];
+    }
+};
 
 // pre-drawn words of one owner, consumed in draw order by the worker
 template <int T>
@@ -53,6 +144,18 @@ struct PreDrawn
     int k;
     __device__ __forceinline__ uint64_t next() { return w[(k++) * T]; }
 };
+
+// first i with m <= thresh[i]: the thresholds of the first nxf-1 xforms are
+// non-decreasing (prefix sums of non-negative weights) and the last is 2^53,
+// so the index is the number of leading thresholds below m
+__device__ __forceinline__ int pick_branchless(const uint64_t* thresh, int nxf, uint64_t m)
+{
+    int x = 0;
+#pragma unroll 4
+    for (int i = 0; i < nxf - 1; ++i)
+        x += m > thresh[i] ? 1 : 0;
+    return x;
+}
 
 template <int D, typename R, bool COLOR, bool SPILL, int T>
 __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* smem)
@@ -72,7 +175,9 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     uint64_t* imem = reinterpret_cast<uint64_t*>(q);
     q += 16 * T * 8;
     uint64_t* irsl = reinterpret_cast<uint64_t*>(q);
-    q += 16 * T * 8;
+    q += kRslWords * T * 8;
+    uint64_t* iabc = reinterpret_cast<uint64_t*>(q);
+    q += 3 * T * 8;
     uint64_t* words = reinterpret_cast<uint64_t*>(q);
     q += (size_t)W * T * 8;
     R* stage = reinterpret_cast<R*>(q);
@@ -81,16 +186,31 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     q += ((size_t)nxf * T * 4 + 15) & ~(size_t)15;
     uint16_t* list = reinterpret_cast<uint16_t*>(q);
     q += ((size_t)nxf * T * 2 + 15) & ~(size_t)15;
+    uint16_t* glist = reinterpret_cast<uint16_t*>(q);
+    q += ((size_t)T * 2 + 15) & ~(size_t)15;
+    uint8_t* gleft = q;
+    q += ((size_t)T + 15) & ~(size_t)15;
     uint32_t* cnt = reinterpret_cast<uint32_t*>(q);         // [2][kSortedMaxXforms]
+    uint32_t* gcnt = cnt + 2 * kSortedMaxXforms;            // [2]
 
     for (int i = 0; i < nxf; ++i)
         xfc[i * T + tid] = 0u;
-    if (tid < 2 * kSortedMaxXforms)
+    if (tid < 2 * kSortedMaxXforms + 2)
         cnt[tid] = 0u;
 
-    DevIsaac<T> rng;
-    rng.mem = imem + tid;
-    rng.rsl = irsl + tid;
+    OwnerRng<T> rng;
+    rng.st.mem = imem + tid;
+    rng.st.rsl = irsl + tid;
+    rng.st.abc = iabc + tid;
+    rng.cnt = 0;
+
+    // words needed between two refill points: the final xform's draws, then
+    // the next choice word and that xform's draws
+    int low = 1 + W;
+    if (h.has_final)
+        low += pg.xf[nxf].rng_words;
+    if (low > kMaxRefillLow)
+        low = kMaxRefillLow;
 
     unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
     R ext_lo[D], ext_hi[D];
@@ -110,7 +230,6 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     const unsigned long long gstride = (unsigned long long)gridDim.x * T;
     volatile unsigned int* vstop = &a.stats->stop;
 
-    // owner state
     unsigned long long s = (unsigned long long)blockIdx.x * T + tid;
     unsigned long long tj = s;
     unsigned long long len = 0;
@@ -152,7 +271,10 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             first = true;
         }
         if (first && tj == s)
-            rng.seed(stream_key(a.seed, s), a.isaac_init);
+        {
+            rng.st.seed(stream_key(a.seed, s), a.isaac_init);
+            rng.cnt = 16;
+        }
         if (*vstop)
             return false;
         len = a.samples - tj * L;
@@ -222,39 +344,71 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     int parity = 0;
     for (;;)
     {
-        // ---- phase A: choose, pre-draw, stage, list
+        // ---- phase A: choose, pre-draw, stage, list, queue refills
         int x = -1;
+        bool want_refill = false;
         if (active)
         {
-            x = pick_xform<R>(pg, rng);
+            x = pick_branchless(pg.thresh, nxf, rng.next() >> 11);
             const int nw = pg.xf[x].rng_words;
             for (int j = 0; j < nw; ++j)
                 words[j * T + tid] = rng.next();
 #pragma unroll
             for (int i = 0; i < D; ++i)
                 stage[i * T + tid] = p[i];
+            want_refill = rng.cnt < low;
         }
         uint32_t* cc = cnt + parity * kSortedMaxXforms;
-        const unsigned int same = __match_any_sync(0xffffffffu, x);
-        const int leader = __ffs(same) - 1;
-        unsigned int base = 0;
-        if (lane == leader && x >= 0)
-            base = atomicAdd(&cc[x], (unsigned int)__popc(same));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (x >= 0)
-            list[x * T + base + __popc(same & ((1u << lane) - 1u))] = (uint16_t)tid;
+        uint32_t* gc = gcnt + parity;
+        {
+            const unsigned int same = __match_any_sync(0xffffffffu, x);
+            const int leader = __ffs(same) - 1;
+            unsigned int base = 0;
+            if (lane == leader && x >= 0)
+                base = atomicAdd(&cc[x], (unsigned int)__popc(same));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (x >= 0)
+                list[x * T + base + __popc(same & ((1u << lane) - 1u))] = (uint16_t)tid;
+        }
+        {
+            const unsigned int rq = __ballot_sync(0xffffffffu, want_refill);
+            unsigned int base = 0;
+            if (lane == 0 && rq)
+                base = atomicAdd(gc, (unsigned int)__popc(rq));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (want_refill)
+            {
+                glist[base + __popc(rq & ((1u << lane) - 1u))] = (uint16_t)tid;
+                gleft[tid] = (uint8_t)rng.cnt;
+            }
+        }
         if (!__syncthreads_or(active))
             break;
 
-        // ---- phase B: uniform-xform chunks
+        // ---- phase B: refills, then uniform-xform chunks
         if (tid < kSortedMaxXforms)
             cnt[(parity ^ 1) * kSortedMaxXforms + tid] = 0u;
-        int total = 0;
+        if (tid == 0)
+            gcnt[parity ^ 1] = 0u;
+        const int ng = (int)*gc;
+        const int gch = (ng + 31) >> 5;
+        int total = gch;
         for (int i = 0; i < nxf; ++i)
             total += (int)((cc[i] + 31u) >> 5);
         for (int ch = warp; ch < total; ch += kWarps)
         {
-            int i = 0, acc = 0;
+            if (ch < gch)
+            {
+                const int k = ch * 32 + lane;
+                if (k < ng)
+                {
+                    const int o = glist[k];
+                    SmemIsaac<T> other{imem + o, irsl + o, iabc + o};
+                    other.refill(gleft[o]);
+                }
+                continue;
+            }
+            int i = 0, acc = gch;
             for (;;)
             {
                 const int n = (int)((cc[i] + 31u) >> 5);
@@ -280,6 +434,8 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
         }
         __syncthreads();
         parity ^= 1;
+        if (want_refill)
+            rng.cnt += 16;
 
         // ---- phase C: owner finishes its sample
         if (!active)
@@ -430,7 +586,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
 }
 
 template <int D, typename R, bool COLOR, bool SPILL, int T>
-__global__ void __launch_bounds__(T) chaos_sorted_kernel(const RenderArgs a)
+__global__ void __launch_bounds__(T, 2) chaos_sorted_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<T>(smem, a.prog, a.prog_bytes);
