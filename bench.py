@@ -244,7 +244,8 @@ def main():
         iters += s.samples_iterated
         launches += 1
         streams, traj_len = s.streams, s.traj_len
-        kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel)
+        kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel) + (
+            " + warp-merged bins" if s.agg else "")
     barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()

@@ -122,6 +122,11 @@ struct ffr_ctx
     unsigned long long isaac_init[16] = {};
     // upper bound of any cell's count (decides when high words are needed)
     unsigned long long count_bound = 0;
+    // autotuner decision (kernel, warp aggregation), valid for spill mode
+    bool tuned = false;
+    bool tuned_spill = false;
+    int tuned_kernel = FFR_KERNEL_PLAIN;
+    int tuned_agg = 0;
     std::string err = "no error";
 
     const Launchers& L() const { return kLaunchers[opts.precision][flame.dims - 1]; }
@@ -260,15 +265,15 @@ int program_words(const ffr_ctx* c)
     return (int)h->rng_words_max;       // same offset in the float header
 }
 
-ffr_status plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* L, int* grid,
-                int* kernel)
+ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint64_t* L,
+                int* grid, int* kernel)
 {
     int bps = 0, block = 0;
     size_t smem = 0;
     const int color = c->flame.color_dims > 0, spill = c->d_hi != nullptr;
     const unsigned int pb = (unsigned int)c->prog_host.size();
     const int nxf = (int)c->flame.xforms.size();
-    int k = c->opts.kernel;
+    int k = kreq;
     if (k != FFR_KERNEL_PLAIN)
     {
         CU(c, c->L().occ_sorted(color, spill, &bps, &block, pb, nxf, program_words(c), &smem));
@@ -307,6 +312,156 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* L, in
     *streams = S;
     *L = len;
     *grid = (int)blocks;
+    return FFR_OK;
+}
+
+// zero a DevStats block on the context stream (+inf/-inf extreme keys)
+ffr_status reset_stats(ffr_ctx* c, DevStats* d)
+{
+    DevStats* head = reinterpret_cast<DevStats*>(new (std::nothrow) unsigned char[sizeof(DevStats)]);
+    if (!head)
+        return fail(c, FFR_ERR_OOM, "out of host memory");
+    std::memset(head, 0, offsetof(DevStats, xf_dist));
+    for (int i = 0; i < kMaxDims; ++i)
+    {
+        head->ext_lo[i] = order_key(INFINITY);
+        head->ext_hi[i] = order_key(-INFINITY);
+    }
+    cudaError_t e = cudaMemcpyAsync(d, head, offsetof(DevStats, xf_dist),
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(d->xf_dist, 0,
+                            sizeof(unsigned long long) * c->flame.xforms.size(), c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);    // head is a host temporary
+    delete[] reinterpret_cast<unsigned char*>(head);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "reset stats");
+    return FFR_OK;
+}
+
+void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint64_t bad_limit,
+               uint64_t S, uint64_t L, unsigned int* counts, unsigned int* hi, double* colors,
+               DevStats* stats, int agg)
+{
+    std::memset(&a, 0, sizeof a);
+    a.prog = c->d_prog;
+    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.nxf = (int)c->flame.xforms.size();
+    a.color_dims = c->flame.color_dims;
+    a.spill = hi != nullptr;
+    a.seed = seed;
+    a.streams = S;
+    a.samples = samples;
+    a.traj_len = L;
+    a.settle = c->opts.settle;
+    a.bad_limit = bad_limit;
+    a.counts = counts;
+    a.hi = hi;
+    a.colors = colors;
+    a.stats = stats;
+    a.cancel = c->d_cancel;
+    a.rng_words = program_words(c);
+    a.agg = agg;
+    std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+}
+
+// Renders this large are autotuned; smaller ones use the static choice.
+constexpr uint64_t kTuneMinSamples = 1ull << 25;
+
+// Autotuner: times a probe render of each (kernel, warp aggregation)
+// candidate into scratch buffers of the same geometry and keeps the fastest
+// for this context.  The probe never touches the context's buffer, so
+// results do not depend on whether tuning ran.
+ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
+{
+    const bool spill = c->d_hi != nullptr;
+    if (c->tuned && c->tuned_spill == spill)
+    {
+        *kernel = c->tuned_kernel;
+        *agg = c->tuned_agg;
+        return FFR_OK;
+    }
+    // static choice: FP32 plain, FP64 sorted where it fits (FP64 pays more
+    // for divergent lanes)
+    *kernel = c->opts.precision == FFR_FP64 ? FFR_KERNEL_AUTO : FFR_KERNEL_PLAIN;
+    *agg = 0;
+    if (samples < kTuneMinSamples)
+        return FFR_OK;
+    const size_t cells = c->flame.cells;
+    const size_t r = (size_t)c->flame.color_dims;
+    const size_t need = cells * 4 * (spill ? 2 : 1) + cells * r * 8 + sizeof(DevStats);
+    size_t fr = 0, tot = 0;
+    CU(c, cudaMemGetInfo(&fr, &tot));
+    if (need > fr / 4)
+        return FFR_OK;
+    unsigned char* buf = nullptr;
+    CU(c, cudaMalloc(&buf, need));
+    unsigned int* pc = reinterpret_cast<unsigned int*>(buf);
+    unsigned int* ph = spill ? pc + cells : nullptr;
+    double* pcol = r ? reinterpret_cast<double*>(buf + cells * 4 * (spill ? 2 : 1)) : nullptr;
+    DevStats* pst = reinterpret_cast<DevStats*>(buf + cells * 4 * (spill ? 2 : 1) + cells * r * 8);
+    const uint64_t P = std::min<uint64_t>(samples, c->opts.precision == FFR_FP64 ? (1u << 22)
+                                                                                 : (1u << 24));
+    float best = 1e30f;
+    int best_k = *kernel, best_a = 0;
+    ffr_status st = FFR_OK;
+    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED})
+    {
+        for (int g : {0, 1})
+        {
+            uint64_t S = 0, L = 0;
+            int grid = 0, kk = 0;
+            st = plan(c, P, k, &S, &L, &grid, &kk);
+            if (st != FFR_OK)
+            {
+                st = FFR_OK;        // candidate does not apply to this flame
+                continue;
+            }
+            RenderArgs a;
+            fill_args(c, a, P, 0x5eedull + (uint64_t)k * 2 + g, ~0ull, S, L, pc, ph, pcol,
+                      pst, g);
+            float ms = 0.f;
+            cudaError_t e = cudaSuccess;
+            for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep)
+            {
+                if ((st = reset_stats(c, pst)) != FFR_OK)
+                    break;
+                e = cudaEventRecord(c->ev0, c->stream);
+                if (e == cudaSuccess)
+                    e = kk == FFR_KERNEL_SORTED ? c->L().sorted(a, grid, c->stream)
+                                                : c->L().render(a, grid, c->stream);
+                if (e == cudaSuccess)
+                    e = cudaEventRecord(c->ev1, c->stream);
+                if (e == cudaSuccess)
+                    e = cudaEventSynchronize(c->ev1);
+                if (e == cudaSuccess)
+                    e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            }
+            if (st != FFR_OK)
+                break;
+            if (e != cudaSuccess)
+            {
+                cudaFree(buf);
+                return cuda_fail(c, e, "autotune probe");
+            }
+            if (ms < best)
+            {
+                best = ms;
+                best_k = kk;
+                best_a = g;
+            }
+        }
+        if (st != FFR_OK)
+            break;
+    }
+    cudaFree(buf);
+    if (st != FFR_OK)
+        return st;
+    c->tuned = true;
+    c->tuned_spill = spill;
+    c->tuned_kernel = *kernel = best_k;
+    c->tuned_agg = *agg = best_a;
     return FFR_OK;
 }
 
@@ -527,7 +682,7 @@ ffr_status ffr_plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* t
     CU(c, cudaSetDevice(c->device));
     uint64_t S = 0, L = 0;
     int grid = 0, kernel = 0;
-    ffr_status s = plan(c, samples, &S, &L, &grid, &kernel);
+    ffr_status s = plan(c, samples, c->opts.kernel, &S, &L, &grid, &kernel);
     if (s != FFR_OK)
         return s;
     if (streams) *streams = S;
@@ -560,43 +715,23 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         if (s != FFR_OK)
             return s;
     }
+    int kreq = c->opts.kernel, agg = 0;
+    if (kreq == FFR_KERNEL_AUTO)
+    {
+        ffr_status ts = autotune(c, samples, &kreq, &agg);
+        if (ts != FFR_OK)
+            return ts;
+    }
     uint64_t S = 0, L = 0;
     int grid = 0, kernel = 0;
-    ffr_status s = plan(c, samples, &S, &L, &grid, &kernel);
+    ffr_status s = plan(c, samples, kreq, &S, &L, &grid, &kernel);
     if (s != FFR_OK)
         return s;
-    // reset device stats: zero, then +inf / -inf extreme keys
-    DevStats head;
-    std::memset(&head, 0, offsetof(DevStats, xf_dist));
-    for (int i = 0; i < kMaxDims; ++i)
-    {
-        head.ext_lo[i] = order_key(INFINITY);
-        head.ext_hi[i] = order_key(-INFINITY);
-    }
-    CU(c, cudaMemcpyAsync(c->d_stats, &head, offsetof(DevStats, xf_dist),
-                          cudaMemcpyHostToDevice, c->stream));
-    CU(c, cudaMemsetAsync(c->d_stats->xf_dist, 0,
-                          sizeof(unsigned long long) * c->flame.xforms.size(), c->stream));
+    if ((s = reset_stats(c, c->d_stats)) != FFR_OK)
+        return s;
     RenderArgs a;
-    std::memset(&a, 0, sizeof a);
-    a.prog = c->d_prog;
-    a.prog_bytes = (unsigned int)c->prog_host.size();
-    a.nxf = (int)c->flame.xforms.size();
-    a.color_dims = c->flame.color_dims;
-    a.spill = c->d_hi != nullptr;
-    a.seed = seed;
-    a.streams = S;
-    a.samples = samples;
-    a.traj_len = L;
-    a.settle = c->opts.settle;
-    a.bad_limit = bad_limit;
-    a.counts = c->d_counts;
-    a.hi = c->d_hi;
-    a.colors = c->d_colors;
-    a.stats = c->d_stats;
-    a.cancel = c->d_cancel;
-    a.rng_words = program_words(c);
-    std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+    fill_args(c, a, samples, seed, bad_limit, S, L, c->d_counts, c->d_hi, c->d_colors,
+              c->d_stats, agg);
     *c->h_cancel = 0u;
     CU(c, cudaEventRecord(c->ev0, c->stream));
     if (kernel == FFR_KERNEL_SORTED)
@@ -654,6 +789,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->traj_len = L;
         st->kernel_ms = ms;
         st->kernel = kernel;
+        st->agg = agg;
     }
     const bool cancelled = hs->cancelled != 0;
     delete hs;

@@ -160,6 +160,40 @@ template <> __device__ __forceinline__ uint64_t to_index<float>(float x)
 template <typename R>
 __device__ __forceinline__ double as_double(R x) { return (double)x; }
 
+// One count for cell bi.  With a.agg, lanes of the warp that bin the same
+// cell in this step are merged by __match_any_sync into one atomic add of
+// their number (hot cells: fixed points, dense attractor cores); otherwise
+// every lane issues its own fire-and-forget add.  With SPILL the returned
+// old value detects the u32 wrap and carries into the high word.
+template <bool SPILL>
+__device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
+{
+    if (a.agg)
+    {
+        const unsigned int same = __match_any_sync(__activemask(), (unsigned long long)bi);
+        if ((int)(threadIdx.x & 31u) != __ffs(same) - 1)
+            return;
+        const unsigned int n = (unsigned int)__popc(same);
+        if (SPILL)
+        {
+            const unsigned int old = atomicAdd(&a.counts[bi], n);
+            if (old + n < old)
+                atomicAdd(&a.hi[bi], 1u);
+        }
+        else
+            atomicAdd(&a.counts[bi], n);
+        return;
+    }
+    if (SPILL)
+    {
+        const unsigned int old = atomicAdd(&a.counts[bi], 1u);
+        if (old == 0xFFFFFFFFu)
+            atomicAdd(&a.hi[bi], 1u);
+    }
+    else
+        atomicAdd(&a.counts[bi], 1u);
+}
+
 template <int D, typename R, bool COLOR, bool SPILL, int BLOCK>
 __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem)
 {
@@ -351,14 +385,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     }
                     if (bi < h.cells)
                     {
-                        if (SPILL)
-                        {
-                            const unsigned int old = atomicAdd(&a.counts[bi], 1u);
-                            if (old == 0xFFFFFFFFu)
-                                atomicAdd(&a.hi[bi], 1u);
-                        }
-                        else
-                            atomicAdd(&a.counts[bi], 1u);
+                        bin_count<SPILL>(a, bi);
                         if (COLOR)
                             for (int i = 0; i < r; ++i)
                                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));

@@ -322,14 +322,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             ++dropped;
             return;
         }
-        if (SPILL)
-        {
-            const unsigned int old = atomicAdd(&a.counts[bi], 1u);
-            if (old == 0xFFFFFFFFu)
-                atomicAdd(&a.hi[bi], 1u);
-        }
-        else
-            atomicAdd(&a.counts[bi], 1u);
+        bin_count<SPILL>(a, bi);
         if (COLOR)
             for (int i = 0; i < r; ++i)
                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));

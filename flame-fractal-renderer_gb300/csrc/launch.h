@@ -49,6 +49,7 @@ struct RenderArgs
     DevStats* stats;
     const volatile unsigned int* cancel;   // host-mapped cancel flag, or null
     int rng_words;                  // largest RNG draw of one xform (sorted kernel)
+    int agg;                        // warp-aggregate increments of equal cells
     unsigned long long isaac_init[16];
 };
 

@@ -70,7 +70,7 @@ class Stats(ctypes.Structure):
                 ("bad_pts", (ctypes.c_double * MAX_DIMS) * MAX_BAD_RECORDS),
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
-                ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32)]
 
 
 _lib = None
@@ -151,6 +151,7 @@ class RenderStats:
     settle: int
     kernel_ms: float
     kernel: int
+    agg: int
 
     @property
     def ok(self) -> bool:
@@ -248,7 +249,7 @@ class BufferRenderer:
             bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
             bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
             streams=st.streams, traj_len=st.traj_len, settle=st.settle,
-            kernel_ms=st.kernel_ms, kernel=st.kernel)
+            kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg)
 
     def plan(self, samples: int):
         s, L = ctypes.c_uint64(), ctypes.c_uint64()

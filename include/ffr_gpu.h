@@ -59,9 +59,11 @@ typedef struct ffr_opts {
     uint32_t abi_version;      /* FFR_ABI_VERSION */
     int32_t device;            /* CUDA device ordinal */
     int32_t precision;         /* ffr_precision */
-    /* render kernel: 0 = automatic, 1 = plain (one thread runs its
-       trajectory's xforms, lanes diverge), 2 = xform-sorted (a CTA groups
-       its threads' points by chosen xform each step); same results */
+    /* render kernel: 0 = automatic (renders of 2^25 samples or more are
+       autotuned once per context over kernel x warp-merged binning on a
+       scratch buffer), 1 = plain (one thread runs its trajectory's xforms,
+       lanes diverge), 2 = xform-sorted (a CTA groups its threads' points by
+       chosen xform each step); every choice gives the same buffer */
     int32_t kernel;
     /* iterations discarded at each trajectory start; the reference uses
        settle_iters<double> = 53 (src/types/constants.hpp:41-47) */
@@ -101,7 +103,7 @@ typedef struct ffr_stats {
     uint64_t settle;
     double kernel_ms;            /* device time of the render kernel(s) */
     int32_t kernel;              /* FFR_KERNEL_PLAIN or FFR_KERNEL_SORTED */
-    int32_t reserved;
+    int32_t agg;                 /* 1: equal-cell increments were warp-merged */
 } ffr_stats;
 
 typedef struct ffr_ctx ffr_ctx;
