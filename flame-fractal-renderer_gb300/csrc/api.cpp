@@ -8,7 +8,10 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <string>
 #include <thread>
 #include <vector>
@@ -369,6 +372,29 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
 // Renders this large are autotuned; smaller ones use the static choice.
 constexpr uint64_t kTuneMinSamples = 1ull << 25;
 
+// Process-wide memory of tuning decisions, keyed by everything the choice
+// depends on: the program bytes (flame + precision), settle, streams and
+// trajectory options, spill mode and device.
+struct TuneKey
+{
+    std::string prog;
+    uint64_t settle, streams, traj_len;
+    int spill, device;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(prog, settle, streams, traj_len, spill, device)
+            < std::tie(o.prog, o.settle, o.streams, o.traj_len, o.spill, o.device);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+TuneKey tune_key(const ffr_ctx* c)
+{
+    return TuneKey{std::string(c->prog_host.begin(), c->prog_host.end()), c->opts.settle,
+                   c->opts.streams, c->opts.traj_len, c->d_hi != nullptr, c->device};
+}
+
 // Autotuner: times a probe render of each (kernel, warp aggregation)
 // candidate into scratch buffers of the same geometry and keeps the fastest
 // for this context.  The probe never touches the context's buffer, so
@@ -381,6 +407,18 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
         *kernel = c->tuned_kernel;
         *agg = c->tuned_agg;
         return FFR_OK;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(tune_key(c));
+        if (it != g_tune_cache.end())
+        {
+            c->tuned = true;
+            c->tuned_spill = spill;
+            c->tuned_kernel = *kernel = it->second.first;
+            c->tuned_agg = *agg = it->second.second;
+            return FFR_OK;
+        }
     }
     // static choice: FP32 plain, FP64 sorted where it fits (FP64 pays more
     // for divergent lanes)
@@ -462,6 +500,10 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
     c->tuned_spill = spill;
     c->tuned_kernel = *kernel = best_k;
     c->tuned_agg = *agg = best_a;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (g_tune_cache.size() > 4096)
+        g_tune_cache.clear();
+    g_tune_cache[tune_key(c)] = {best_k, best_a};
     return FFR_OK;
 }
 
