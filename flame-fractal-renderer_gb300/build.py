@@ -64,18 +64,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
     hdrs = _headers()
     nv_common = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
                  "-I", CSRC, "-I", INCLUDE]
-    cxx_common = ["g++", "-std=c++17", "-O2", "-fPIC",
+    cxx_common = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off",
                   "-Wall", "-Wextra", "-I", CSRC, "-I", INCLUDE,
                   "-I", os.path.join(cuda, "include")]
     jobs = []   # (target, deps, cmd)
     for p in (0, 1):
         for d in (1, 2, 3):
-            obj = os.path.join(OUT, f"chaos_p{p}_d{d}.o")
-            src = os.path.join(CSRC, "chaos_inst.cu")
-            extra = ["--fmad=false"] if p == 0 else []
-            jobs.append((obj, [src] + hdrs,
-                         [nvcc, *nv_common, *extra, f"-DFFR_P={p}", f"-DFFR_D={d}",
-                          "-c", src, "-o", obj]))
+            for kind in (0, 1):
+                obj = os.path.join(OUT, f"chaos_p{p}_d{d}_k{kind}.o")
+                src = os.path.join(CSRC, "chaos_inst.cu")
+                extra = ["--fmad=false"] if p == 0 else []
+                jobs.append((obj, [src] + hdrs,
+                             [nvcc, *nv_common, *extra, f"-DFFR_P={p}", f"-DFFR_D={d}",
+                              f"-DFFR_KIND={kind}", "-c", src, "-o", obj]))
     for name in ("buffer_kernels", "noalloc"):
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(OUT, name + ".o")

@@ -1,12 +1,14 @@
 // Instantiates the chaos kernels for one (precision, dims) pair; compiled
-// once per pair with -DFFR_P=<0|1> -DFFR_D=<1|2|3>.  The FP64 objects are
+// once per pair and kind with -DFFR_P=<0|1> -DFFR_D=<1|2|3>
+// -DFFR_KIND=<0|1> (0: plain render, step and trace kernels; 1: the
+// xform-sorted render kernel), so the objects compile in parallel.  The FP64 objects are
 // built with --fmad=false so no multiply-add is contracted: the reference
 // (and the oracle) round every product and sum separately.
 #include "chaos_kernel.cuh"
 #include "chaos_sorted.cuh"
 
-#if !defined(FFR_P) || !defined(FFR_D)
-#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3>"
+#if !defined(FFR_P) || !defined(FFR_D) || !defined(FFR_KIND)
+#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3> -DFFR_KIND=<0|1>"
 #endif
 
 #define FFR_CAT2(a, b, c, d) a##_p##b##_d##c##d
@@ -21,13 +23,15 @@ using Real = double;
 using Real = float;
 #endif
 
+#if FFR_KIND == 0
+
 constexpr int kBlock = 128;
 
-template <bool C, bool S>
+template <bool C>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf);
-    auto k = chaos_kernel<FFR_D, Real, C, S, kBlock>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -36,11 +40,11 @@ static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <bool C, bool S>
+template <bool C>
 static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, size_t* smem_out)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf);
-    auto k = chaos_kernel<FFR_D, Real, C, S, kBlock>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -49,82 +53,18 @@ static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, size_t* s
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kBlock, smem);
 }
 
-constexpr int kSortedBlock = 256;
-
-template <bool C, bool S>
-static cudaError_t launch_sorted_one(const RenderArgs& a, int grid, cudaStream_t st)
-{
-    const size_t smem = sorted_smem_bytes<kSortedBlock>(
-        a.prog_bytes, a.nxf, a.rng_words, FFR_D, (int)sizeof(Real));
-    auto k = chaos_sorted_kernel<FFR_D, Real, C, S, kSortedBlock>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    k<<<grid, kSortedBlock, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-template <bool C, bool S>
-static cudaError_t occ_sorted_one(int* bps, unsigned int prog_bytes, int nxf, int words,
-                                  size_t* smem_out)
-{
-    const size_t smem = sorted_smem_bytes<kSortedBlock>(prog_bytes, nxf, words, FFR_D,
-                                                        (int)sizeof(Real));
-    auto k = chaos_sorted_kernel<FFR_D, Real, C, S, kSortedBlock>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess)
-        return e;
-    *smem_out = smem;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kSortedBlock, smem);
-}
-
-cudaError_t FFR_NAME(launch_sorted)(const RenderArgs& a, int grid, cudaStream_t st)
-{
-    if (a.color_dims > 0)
-        return a.spill ? launch_sorted_one<true, true>(a, grid, st)
-                       : launch_sorted_one<true, false>(a, grid, st);
-    return a.spill ? launch_sorted_one<false, true>(a, grid, st)
-                   : launch_sorted_one<false, false>(a, grid, st);
-}
-
-cudaError_t FFR_NAME(occupancy_sorted)(int color, int spill, int* blocks_per_sm, int* block,
-                                       unsigned int prog_bytes, int nxf, int words,
-                                       size_t* smem)
-{
-    *block = kSortedBlock;
-    if (nxf > kSortedMaxXforms)
-    {
-        *blocks_per_sm = 0;
-        return cudaSuccess;
-    }
-    if (color)
-        return spill ? occ_sorted_one<true, true>(blocks_per_sm, prog_bytes, nxf, words, smem)
-                     : occ_sorted_one<true, false>(blocks_per_sm, prog_bytes, nxf, words, smem);
-    return spill ? occ_sorted_one<false, true>(blocks_per_sm, prog_bytes, nxf, words, smem)
-                 : occ_sorted_one<false, false>(blocks_per_sm, prog_bytes, nxf, words, smem);
-}
-
 cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t st)
 {
-    const bool color = a.color_dims > 0;
-    if (color)
-        return a.spill ? launch_one<true, true>(a, grid, st)
-                       : launch_one<true, false>(a, grid, st);
-    return a.spill ? launch_one<false, true>(a, grid, st)
-                   : launch_one<false, false>(a, grid, st);
+    return a.color_dims > 0 ? launch_one<true>(a, grid, st) : launch_one<false>(a, grid, st);
 }
 
 cudaError_t FFR_NAME(occupancy)(int color, int spill, int* blocks_per_sm, int* block,
                                 unsigned int prog_bytes, int nxf, size_t* smem)
 {
+    (void)spill;
     *block = kBlock;
-    if (color)
-        return spill ? occ_one<true, true>(blocks_per_sm, prog_bytes, nxf, smem)
-                     : occ_one<true, false>(blocks_per_sm, prog_bytes, nxf, smem);
-    return spill ? occ_one<false, true>(blocks_per_sm, prog_bytes, nxf, smem)
-                 : occ_one<false, false>(blocks_per_sm, prog_bytes, nxf, smem);
+    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, smem)
+                 : occ_one<false>(blocks_per_sm, prog_bytes, nxf, smem);
 }
 
 cudaError_t FFR_NAME(launch_step)(const StepArgs& a, cudaStream_t st)
@@ -155,5 +95,61 @@ cudaError_t FFR_NAME(launch_trace)(const TraceArgs& a, cudaStream_t st)
     k<<<1, 1, smem, st>>>(a);
     return cudaGetLastError();
 }
+
+#else
+
+constexpr int kSortedBlock = 256;
+
+template <bool C>
+static cudaError_t launch_sorted_one(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    const size_t smem = sorted_smem_bytes<kSortedBlock>(
+        a.prog_bytes, a.nxf, a.rng_words, FFR_D, (int)sizeof(Real));
+    auto k = chaos_sorted_kernel<FFR_D, Real, C, kSortedBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, kSortedBlock, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool C>
+static cudaError_t occ_sorted_one(int* bps, unsigned int prog_bytes, int nxf, int words,
+                                  size_t* smem_out)
+{
+    const size_t smem = sorted_smem_bytes<kSortedBlock>(prog_bytes, nxf, words, FFR_D,
+                                                        (int)sizeof(Real));
+    auto k = chaos_sorted_kernel<FFR_D, Real, C, kSortedBlock>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    *smem_out = smem;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kSortedBlock, smem);
+}
+
+cudaError_t FFR_NAME(launch_sorted)(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    return a.color_dims > 0 ? launch_sorted_one<true>(a, grid, st)
+                            : launch_sorted_one<false>(a, grid, st);
+}
+
+cudaError_t FFR_NAME(occupancy_sorted)(int color, int spill, int* blocks_per_sm, int* block,
+                                       unsigned int prog_bytes, int nxf, int words,
+                                       size_t* smem)
+{
+    *block = kSortedBlock;
+    if (nxf > kSortedMaxXforms)
+    {
+        *blocks_per_sm = 0;
+        return cudaSuccess;
+    }
+    (void)spill;
+    return color ? occ_sorted_one<true>(blocks_per_sm, prog_bytes, nxf, words, smem)
+                 : occ_sorted_one<false>(blocks_per_sm, prog_bytes, nxf, words, smem);
+}
+
+#endif
 
 } // namespace ffr

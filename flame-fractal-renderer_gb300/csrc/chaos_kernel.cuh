@@ -163,9 +163,8 @@ __device__ __forceinline__ double as_double(R x) { return (double)x; }
 // One count for cell bi.  With a.agg, lanes of the warp that bin the same
 // cell in this step are merged by __match_any_sync into one atomic add of
 // their number (hot cells: fixed points, dense attractor cores); otherwise
-// every lane issues its own fire-and-forget add.  With SPILL the returned
+// every lane issues its own fire-and-forget add.  With a.spill the returned
 // old value detects the u32 wrap and carries into the high word.
-template <bool SPILL>
 __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
 {
     if (a.agg)
@@ -174,7 +173,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
         if ((int)(threadIdx.x & 31u) != __ffs(same) - 1)
             return;
         const unsigned int n = (unsigned int)__popc(same);
-        if (SPILL)
+        if (a.spill)
         {
             const unsigned int old = atomicAdd(&a.counts[bi], n);
             if (old + n < old)
@@ -184,7 +183,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
             atomicAdd(&a.counts[bi], n);
         return;
     }
-    if (SPILL)
+    if (a.spill)
     {
         const unsigned int old = atomicAdd(&a.counts[bi], 1u);
         if (old == 0xFFFFFFFFu)
@@ -194,7 +193,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
         atomicAdd(&a.counts[bi], 1u);
 }
 
-template <int D, typename R, bool COLOR, bool SPILL, int BLOCK>
+template <int D, typename R, bool COLOR, int BLOCK>
 __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem)
 {
     using T = RealTraits<R>;
@@ -385,7 +384,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     }
                     if (bi < h.cells)
                     {
-                        bin_count<SPILL>(a, bi);
+                        bin_count(a, bi);
                         if (COLOR)
                             for (int i = 0; i < r; ++i)
                                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));
@@ -462,13 +461,13 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     }
 }
 
-template <int D, typename R, bool COLOR, bool SPILL, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) chaos_kernel(const RenderArgs a)
+template <int D, typename R, bool COLOR, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 4) chaos_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
     __syncthreads();
-    chaos_body<D, R, COLOR, SPILL, BLOCK>(a, smem);
+    chaos_body<D, R, COLOR, BLOCK>(a, smem);
 }
 
 // XForm::applyIteration on a batch of points; point k uses stream

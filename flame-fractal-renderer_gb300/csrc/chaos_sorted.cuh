@@ -157,7 +157,7 @@ __device__ __forceinline__ int pick_branchless(const uint64_t* thresh, int nxf, 
     return x;
 }
 
-template <int D, typename R, bool COLOR, bool SPILL, int T>
+template <int D, typename R, bool COLOR, int T>
 __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* smem)
 {
     using Tr = RealTraits<R>;
@@ -322,7 +322,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             ++dropped;
             return;
         }
-        bin_count<SPILL>(a, bi);
+        bin_count(a, bi);
         if (COLOR)
             for (int i = 0; i < r; ++i)
                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));
@@ -578,13 +578,13 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     }
 }
 
-template <int D, typename R, bool COLOR, bool SPILL, int T>
+template <int D, typename R, bool COLOR, int T>
 __global__ void __launch_bounds__(T, 2) chaos_sorted_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<T>(smem, a.prog, a.prog_bytes);
     __syncthreads();
-    sorted_body<D, R, COLOR, SPILL, T>(a, smem);
+    sorted_body<D, R, COLOR, T>(a, smem);
 }
 
 } // namespace ffr

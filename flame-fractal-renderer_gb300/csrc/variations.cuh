@@ -37,6 +37,21 @@ template <> struct RealTraits<double>
     __device__ static __forceinline__ double sqrt_(double x) { return sqrt(x); }
     __device__ static __forceinline__ double fabs_(double x) { return fabs(x); }
     __device__ static __forceinline__ double recip_(double x) { return 1.0 / x; }
+    static constexpr double pi_4 = 0.78539816339744830962;      // M_PI_4
+    __device__ static __forceinline__ double tan_(double x) { return tan(x); }
+    __device__ static __forceinline__ double log_(double x) { return log(x); }
+    __device__ static __forceinline__ double log10_(double x) { return log10(x); }
+    __device__ static __forceinline__ double exp_(double x) { return exp(x); }
+    __device__ static __forceinline__ double pow_(double x, double y) { return pow(x, y); }
+    __device__ static __forceinline__ double sinh_(double x) { return sinh(x); }
+    __device__ static __forceinline__ double cosh_(double x) { return cosh(x); }
+    __device__ static __forceinline__ double acos_(double x) { return acos(x); }
+    __device__ static __forceinline__ double floor_(double x) { return floor(x); }
+    __device__ static __forceinline__ double fmod_(double x, double y) { return fmod(x, y); }
+    __device__ static __forceinline__ double rint_(double x) { return rint(x); }
+    __device__ static __forceinline__ double copysign_(double x, double y) { return copysign(x, y); }
+    __device__ static __forceinline__ double hypot_(double x, double y) { return hypot(x, y); }
+    __device__ static __forceinline__ double trunc_(double x) { return trunc(x); }
 };
 
 template <> struct RealTraits<float>
@@ -81,14 +96,31 @@ template <> struct RealTraits<float>
     __device__ static __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     __device__ static __forceinline__ float fabs_(float x) { return fabsf(x); }
     __device__ static __forceinline__ float recip_(float x) { return __fdividef(1.0f, x); }
+    static constexpr float pi_4 = 0.78539816339744830962f;
+    __device__ static __forceinline__ float tan_(float x) { return tanf(x); }
+    __device__ static __forceinline__ float log_(float x) { return logf(x); }
+    __device__ static __forceinline__ float log10_(float x) { return log10f(x); }
+    __device__ static __forceinline__ float exp_(float x) { return expf(x); }
+    __device__ static __forceinline__ float pow_(float x, float y) { return powf(x, y); }
+    __device__ static __forceinline__ float sinh_(float x) { return sinhf(x); }
+    __device__ static __forceinline__ float cosh_(float x) { return coshf(x); }
+    __device__ static __forceinline__ float acos_(float x) { return acosf(x); }
+    __device__ static __forceinline__ float floor_(float x) { return floorf(x); }
+    __device__ static __forceinline__ float fmod_(float x, float y) { return fmodf(x, y); }
+    __device__ static __forceinline__ float rint_(float x) { return rintf(x); }
+    __device__ static __forceinline__ float copysign_(float x, float y) { return copysignf(x, y); }
+    __device__ static __forceinline__ float hypot_(float x, float y) { return hypotf(x, y); }
+    __device__ static __forceinline__ float trunc_(float x) { return truncf(x); }
 };
 
 // t[i] for a run-time i without dynamic register indexing
 template <int D, typename R>
 __device__ __forceinline__ R coord(const R* t, int i)
 {
-    if (D <= 2)
-        return t[i & 1];
+    if (D == 1)
+        return t[0];
+    if (D == 2)
+        return t[(i & 1) & (D - 1)];
     R r = t[0];
 #pragma unroll
     for (int k = 1; k < D; ++k)
@@ -96,86 +128,652 @@ __device__ __forceinline__ R coord(const R* t, int i)
     return r;
 }
 
-// one variation: o = V(t)
+// Point::normsum<2> (point.hpp:300-307): squares summed in coordinate order
+template <int D, typename R>
+__device__ __forceinline__ R nsq(const R* t)
+{
+    R r = t[0] * t[0];
+#pragma unroll
+    for (int i = 1; i < D; ++i)
+        r += t[i] * t[i];
+    return r;
+}
+
+// Point::norm<2> (point.hpp:270-290): |x| in 1-D, else sqrt(normsum<2>)
+template <int D, typename R>
+__device__ __forceinline__ R n2(const R* t)
+{
+    if (D == 1)
+        return RealTraits<R>::fabs_(t[0]);
+    return RealTraits<R>::sqrt_(nsq<D>(t));
+}
+
+// Point::normsum(p) (point.hpp:325-331)
+template <int D, typename R>
+__device__ __forceinline__ R normsum_p(const R* t, R p)
+{
+    using T = RealTraits<R>;
+    R r = T::pow_(T::fabs_(t[0]), p);
+#pragma unroll
+    for (int i = 1; i < D; ++i)
+        r += T::pow_(T::fabs_(t[i]), p);
+    return r;
+}
+
+// FlameRNG::randGaussianPair (flame_rng.hpp:115-140), first value
+template <typename R, typename Rng>
+__device__ __forceinline__ R rand_gauss(Rng& rng)
+{
+    using T = RealTraits<R>;
+    const R u1 = T::unit(rng.next());
+    const R u2 = (R(2) * T::pi) * T::unit(rng.next());
+    const R r = T::sqrt_(R(-2) * T::log_(u1));
+    R s, c;
+    T::sincos_(u2, &s, &c);
+    return r * c;
+}
+
+// FlameRNG::randDirection<dims> (flame_rng.hpp:171-217)
+template <int D, typename R, typename Rng>
+__device__ __forceinline__ void rand_dir(Rng& rng, R* d)
+{
+    using T = RealTraits<R>;
+    if (D == 1)
+    {
+        d[0] = T::copysign_(R(1), T::unit(rng.next()) - R(0.5));
+    }
+    else if (D == 2)
+    {
+        const R a = (R(2) * T::pi) * T::unit(rng.next());
+        R sa, ca;
+        T::sincos_(a, &sa, &ca);
+        d[0] = ca;
+        d[D > 1 ? 1 : 0] = sa;
+    }
+    else
+    {
+        const R u = R(2) * T::unit(rng.next()) - R(1);
+        const R tt = (R(2) * T::pi) * T::unit(rng.next());
+        const R r = T::sqrt_(R(1) - u * u);
+        R st, ct;
+        T::sincos_(tt, &st, &ct);
+        d[0] = r * ct;
+        d[D > 1 ? 1 : 0] = r * st;
+        d[D > 2 ? 2 : 0] = u;
+    }
+}
+
+// one variation: o = V(t).  Restates each class of
+// src/variations/variations.hpp (line numbers in the case comments) in the
+// reference's operation order; Point / k is multiplication by (1/k), as
+// Point::operator/= does (src/types/point.hpp:127-131).  RNG draws go
+// through rng.next() in the reference's order (FlameRNG,
+// src/rng/flame_rng.hpp).
 template <int D, typename R, typename Rng>
 __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng)
 {
     using T = RealTraits<R>;
     const int ax = v.axis_x, ay = v.axis_y;
-    R x2 = R(0), y2 = R(0);
-    switch (v.type)
-    {
-    case V_LINEAR:                       // variations.hpp:169-177
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-            o[i] = t[i];
-        return;
-    case V_SINUSOIDAL:                   // variations.hpp:183-191
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-            o[i] = T::sin_(t[i]);
-        return;
-    case V_SPHERICAL:                    // variations.hpp:197-208
-    {
-        R r2 = t[0] * t[0];
-#pragma unroll
-        for (int i = 1; i < D; ++i)
-            r2 += t[i] * t[i];
-        const R r = T::recip_(r2 + T::eps);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-            o[i] = t[i] * r;
-        return;
+    R* out = o;
+
+    const R* P = v.p;
+    R x, y, r, a, s, c, X = R(0), Y = R(0), d;
+        if (v.type < kFirst2D) {
+        switch (v.type) {
+        case V_LINEAR: /* 169-177 */
+            for (int i = 0; i < D; ++i) out[i] = t[i];
+            return;
+        case V_SINUSOIDAL: /* 183-191 */
+            for (int i = 0; i < D; ++i) out[i] = T::sin_(t[i]);
+            return;
+        case V_SPHERICAL: /* 197-208 */
+            r = T::recip_(nsq<D>(t) + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_BENT: /* 216-240: p = neg[dims], pos[dims] */
+            for (int i = 0; i < D; ++i)
+                out[i] = t[i] < R(0.0) ? t[i] * P[i] : t[i] * P[D + i];
+            return;
+        case V_RECTANGLES: /* 245-270 */
+            for (int i = 0; i < D; ++i)
+                out[i] = P[i] == R(0.0) ? t[i]
+                    : (R(2.0) * T::floor_(t[i] / P[i]) + R(1.0)) * P[i] - t[i];
+            return;
+        case V_FISHEYE: /* 275-292: p = addval */
+            r = T::recip_(n2<D>(t) + P[0]);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_BUBBLE: /* 297-314 */
+            r = T::recip_(nsq<D>(t) + P[0]);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_NOISE: { /* 319-330 */
+            R dir[D];
+            r = T::unit(rng.next());
+            rand_dir<D, R>(rng, dir);
+            for (int i = 0; i < D; ++i) out[i] = (t[i] * dir[i]) * r;
+            return;
+        }
+        case V_BLUR: { /* 335-347 */
+            R dir[D];
+            r = T::unit(rng.next());
+            rand_dir<D, R>(rng, dir);
+            for (int i = 0; i < D; ++i) out[i] = dir[i] * r;
+            return;
+        }
+        case V_GAUSSIAN_BLUR: /* 352-364 */
+        case V_PRE_BLUR: { /* 434-446 */
+            R dir[D];
+            r = rand_gauss<R>(rng);
+            rand_dir<D, R>(rng, dir);
+            for (int i = 0; i < D; ++i) out[i] = dir[i] * r;
+            return;
+        }
+        case V_SQUARE_NOISE: /* 369-378, randPoint2 */
+            for (int i = 0; i < D; ++i) out[i] = T::unit(rng.next()) - R(0.5);
+            return;
+        case V_SEPARATION: /* 383-405: p = sep^2[dims], inside[dims] */
+            for (int i = 0; i < D; ++i) {
+                s = T::copysign_(R(1.0), t[i]);
+                out[i] = s * (T::sqrt_(t[i] * t[i] + P[i]) - s * P[D + i]);
+            }
+            return;
+        case V_SPLITS: /* 410-429 */
+            for (int i = 0; i < D; ++i) {
+                s = T::copysign_(R(1.0), t[i]);
+                out[i] = t[i] + s * P[i];
+            }
+            return;
+        case V_MODULUS: /* 451-471: p = 2*params, 1/(2*params) */
+            for (int i = 0; i < D; ++i)
+                out[i] = t[i] - P[i] * T::floor_(t[i] * P[D + i] + R(0.5));
+            return;
+        case V_CELLN: /* 476-505: p = sizes, 1/sizes */
+            for (int i = 0; i < D; ++i) {
+                R fx = T::floor_(t[i] * P[D + i]);
+                R dx = t[i] - fx * P[i];
+                R xs = T::copysign_(R(2.0), fx);
+                R x2 = fx * xs;
+                x2 -= (R)(fx < 0);
+                out[i] = dx + x2 * P[i];
+            }
+            return;
+        case V_SPHERICAL_P: /* 2312-2328 */
+            r = T::recip_(normsum_p<D>(t, P[0]) + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_UNIT_SPHERE: /* 2333-2342 */
+            r = T::recip_(n2<D>(t) + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_UNIT_SPHERE_P: /* 2347-2363: norm(p) = T::pow_(normsum, 1/p) */
+            r = T::recip_(T::pow_(normsum_p<D>(t, P[0]), R(1.0) / P[0]) + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        case V_UNIT_CUBE: { /* 2368-2376: norm<0> */
+            R m = T::fabs_(t[0]);
+            if (D > 1)
+                for (int i = 1; i < D; ++i) {
+                    R q = T::fabs_(t[i]);
+                    m = (m < q) ? q : m;
+                }
+            r = T::recip_(m + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+            return;
+        }
+        default:
+            for (int i = 0; i < D; ++i) out[i] = (R(0) / R(0));
+            return;
+        }
     }
-    case V_SWIRL:                        // variations.hpp:509-522
-    {
-        const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-        const R r = x * x + y * y;
-        R s, c;
-        T::sincos_(r, &s, &c);
-        x2 = x * s - y * c;
-        y2 = x * c + y * s;
-        break;
-    }
-    case V_HORSESHOE:                    // variations.hpp:527-540
-    {
-        const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-        const R r = T::recip_(T::sqrt_(x * x + y * y) + T::eps);
-        x2 = ((x - y) * (x + y)) * r;
-        y2 = (R(2) * x * y) * r;
-        break;
-    }
-    case V_POLAR:                        // variations.hpp:545-555
-    {
-        const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-        const R a = T::atan2_(y, x);
-        const R r = T::sqrt_(x * x + y * y);
-        x2 = a * T::inv_pi;
-        y2 = r - R(1);
-        break;
-    }
-    case V_JULIA:                        // variations.hpp:807-819
-    {
-        const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-        const R a = R(0.5) * T::atan2_(y, x) + (R)(rng.next() & 1u) * T::pi;
-        R s, c;
+    x = coord<D>(t, ax);
+    y = coord<D>(t, ay);
+#define R2SQ (x * x + y * y)
+#define R2 T::sqrt_(x * x + y * y)
+#define ANG T::atan2_(y, x)
+    switch (v.type) {
+    case V_SWIRL: /* 509-522 */
+        r = R2SQ; T::sincos_(r, &s, &c);
+        X = x * s - y * c; Y = x * c + y * s; break;
+    case V_HORSESHOE: /* 527-540 */
+        r = T::recip_(R2 + T::eps);
+        X = ((x - y) * (x + y)) * r; Y = (R(2.0) * x * y) * r; break;
+    case V_POLAR: /* 545-555 */
+        a = ANG; r = R2; X = a * T::inv_pi; Y = r - R(1.0); break;
+    case V_POLAR2: /* 561-570 */
+        X = ANG; Y = T::log_(R2SQ); break;
+    case V_HANDKERCHIEF: /* 575-585 */
+        a = ANG; r = R2; X = T::sin_(a + r) * r; Y = T::cos_(a - r) * r; break;
+    case V_HEART: /* 590-602 */
+        a = ANG; r = R2; T::sincos_(r * a, &s, &c); X = s * r; Y = (-c) * r; break;
+    case V_DISC: /* 607-619 */
+        a = ANG; r = R2; T::sincos_(T::pi * r, &s, &c); X = s * a; Y = c * a; break;
+    case V_DISC2: /* 624-655: p = rotpi, cosadd, sinadd */
+        d = P[0] * (x + y); T::sincos_(d, &s, &c); a = ANG;
+        X = (c + P[1]) * a; Y = (s + P[2]) * a; break;
+    case V_WAVES: /* 660-680: p = xf, xs, yf, ys */
+        X = x + P[1] * T::sin_(y * P[0]); Y = y + P[3] * T::sin_(x * P[2]); break;
+    case V_FAN: { /* 685-709: p = dx, dy */
+        R dx2 = P[0] * R(0.5);
+        a = ANG;
+        R m = T::copysign_(R(1.0), dx2 - T::fmod_(a + P[1], P[0]));
+        a += m * dx2;
         T::sincos_(a, &s, &c);
-        const R r = T::sqrt_(x * x + y * y);
-        x2 = c * r;
-        y2 = s * r;
+        r = R2;
+        X = c * r; Y = s * r; break;
+    }
+    case V_RINGS: /* 714-733: p = dx */
+        r = R2; s = y / r; c = x / r;
+        r = T::fmod_(r + P[0], R(2.0) * P[0]) - P[0] + r * (R(1.0) - P[0]);
+        X = c * r; Y = s * r; break;
+    case V_SPIRAL: { /* 738-752 */
+        R sa, ca, sr, cr;
+        r = R2; sa = y / r; ca = x / r;
+        T::sincos_(r, &sr, &cr);
+        R r1 = T::recip_(r + T::eps);
+        X = (ca + sr) * r1; Y = (sa - cr) * r1; break;
+    }
+    case V_HYPERBOLIC: /* 757-767 */
+        r = R2; s = y / r; c = x / r;
+        X = s / (r + T::eps); Y = c * r; break;
+    case V_DIAMOND: { /* 772-784 */
+        R sr, cr;
+        r = R2; s = y / r; c = x / r;
+        T::sincos_(r, &sr, &cr);
+        X = s * cr; Y = c * sr; break;
+    }
+    case V_EX: { /* 789-803 */
+        a = ANG; r = R2;
+        R n0 = T::sin_(a + r), n1 = T::cos_(a - r);
+        R m0 = n0 * n0 * n0 * r, m1 = n1 * n1 * n1 * r;
+        X = m0 + m1; Y = m0 - m1; break;
+    }
+    case V_JULIA: /* 807-819 */
+        a = R(0.5) * T::atan2_(y, x) + (R)(rng.next() & 1u) * T::pi;
+        T::sincos_(a, &s, &c);
+        r = R2;
+        X = c * r; Y = s * r; break;
+    case V_EXPONENTIAL: /* 825-838 */
+        d = T::exp_(x - R(1.0)); T::sincos_(T::pi * y, &s, &c);
+        X = c * d; Y = s * d; break;
+    case V_POWER: /* 843-853 */
+        r = R2; s = y / r; c = x / r; d = T::pow_(r, s);
+        X = c * d; Y = s * d; break;
+    case V_COSINE: /* 858-870 */
+        T::sincos_(x * T::pi, &s, &c);
+        X = c * T::cosh_(y); Y = (-s) * T::sinh_(y); break;
+    case V_BLOB: /* 875-896: p = mid, amp, waves */
+        r = R2; s = y / r; c = x / r; a = ANG;
+        r *= P[0] + P[1] * T::sin_(P[2] * a);
+        X = c * r; Y = s * r; break;
+    case V_PDJ: /* 901-925: p = a, b, c, d */
+        X = T::sin_(P[0] * y) - T::cos_(P[1] * x); Y = T::sin_(P[2] * x) - T::cos_(P[3] * y); break;
+    case V_CYLINDER: /* 930-938 */
+        X = T::sin_(x); Y = y; break;
+    case V_PERSPECTIVE: /* 943-962: p = dist, vsin, vfcos */
+        d = T::recip_(P[0] - y * P[1]);
+        X = (P[0] * x) * d; Y = (P[2] * y) * d; break;
+    case V_JULIAN: { /* 967-989: p = abspower, invpower, cn */
+        int32_t tt = (int32_t)T::trunc_(P[0] * T::unit(rng.next()));
+        a = (T::atan2_(y, x) + (R(2.0) * T::pi) * tt) * P[1];
+        r = T::pow_(R2SQ, P[2]);
+        T::sincos_(a, &s, &c);
+        X = c * r; Y = s * r; break;
+    }
+    case V_JULIASCOPE: { /* 994-1018 */
+        int32_t tt = (int32_t)T::trunc_(P[0] * T::unit(rng.next()));
+        R dir = T::copysign_(R(1.0), T::unit(rng.next()) - R(0.5));
+        a = ((R(2.0) * T::pi) * tt + dir * T::atan2_(y, x)) * P[1];
+        r = T::pow_(R2SQ, P[2]);
+        T::sincos_(a, &s, &c);
+        X = c * r; Y = s * r; break;
+    }
+    case V_RADIAL_BLUR: { /* 1023-1045: p = spin, zoom, flam3weight */
+        R g = P[2] * rand_gauss<R>(rng);
+        R ra = R2;
+        a = T::atan2_(y, x) + P[0] * g;
+        T::sincos_(a, &s, &c);
+        R rz = P[1] * g - R(1.0);
+        X = c * ra + x * rz; Y = s * ra + y * rz; break;
+    }
+    case V_PIE: { /* 1050-1072: p = slices, rotation, thickness, invslices2pi */
+        int32_t sl = (int32_t)(T::unit(rng.next()) * P[0] + R(0.5));
+        a = P[1] + (sl + T::unit(rng.next()) * P[2]) * P[3];
+        r = T::unit(rng.next());
+        T::sincos_(a, &s, &c);
+        X = c * r; Y = s * r; break;
+    }
+    case V_NGON: { /* 1077-1102: p = powerval, angle, corners, circle, invangle */
+        r = T::pow_(R2SQ, P[0]);
+        R theta = T::atan2_(y, x);
+        R phi = theta - P[1] * T::floor_(theta * P[4]);
+        phi -= (phi > P[1] * R(0.5) ? R(1.0) : R(0.0)) * P[1];
+        R amp = P[2] * (T::recip_(T::cos_(phi) + T::eps) - R(1.0)) + P[3];
+        amp /= r + T::eps;
+        X = x * amp; Y = y * amp; break;
+    }
+    case V_CURL: { /* 1107-1129: p = c1, c2 */
+        R re = R(1.0) + P[0] * x + P[1] * (x * x - y * y);
+        R im = P[0] * y + R(2.0) * P[1] * x * y;
+        r = T::recip_(re * re + im * im + T::eps);
+        X = (x * re + y * im) * r; Y = (y * re - x * im) * r; break;
+    }
+    case V_ARCH: /* 1134-1151: p = flam3weight */
+        a = P[0] * T::unit(rng.next()) * T::pi;
+        T::sincos_(a, &s, &c);
+        X = s; Y = s * s / c; break;
+    case V_TANGENT: /* 1156-1166 */
+        X = T::sin_(x) / T::cos_(y); Y = T::tan_(y); break;
+    case V_RAYS: /* 1172-1191 */
+        a = P[0] * T::unit(rng.next()) * T::pi;
+        r = P[0] / (R2SQ + T::eps);
+        d = T::tan_(a) * r;
+        X = T::cos_(x) * d; Y = T::sin_(y) * d; break;
+    case V_BLADE: { /* 1196-1213 */
+        R sr, cr;
+        r = T::unit(rng.next()) * P[0] * R2;
+        T::sincos_(r, &sr, &cr);
+        X = (cr + sr) * x; Y = (cr - sr) * x; break;
+    }
+    case V_SECANT: { /* 1218-1235 */
+        R cr = T::cos_(P[0] * R2);
+        R icr = R(1.0) / cr;
+        R sg = T::copysign_(R(1.0), -cr);
+        X = x; Y = icr + sg; break;
+    }
+    case V_TWINTRIAN: { /* 1240-1260 */
+        R sr, cr;
+        r = T::unit(rng.next()) * P[0] * R2;
+        T::sincos_(r, &sr, &cr);
+        R diff = T::log10_(sr * sr) + cr;
+        if (T::fabs_(diff) > T::bad || (diff != diff))
+            diff = -R(30.0);
+        X = diff * x; Y = (diff - sr * T::pi) * x; break;
+    }
+    case V_CROSS: /* 1265-1277 */
+        s = x * x - y * y;
+        r = T::sqrt_(T::recip_(s * s + T::eps));
+        X = x * r; Y = y * r; break;
+    case V_EXP: /* 1282-1295 */
+        d = T::exp_(x); T::sincos_(y, &s, &c);
+        X = c * d; Y = s * d; break;
+    case V_LOG: /* 1300-1308 */
+        X = T::log_(R2SQ); Y = T::atan2_(y, x); break;
+    case V_SIN: /* 1313-1327 */
+        T::sincos_(x, &s, &c);
+        X = s * T::cosh_(y); Y = c * T::sinh_(y); break;
+    case V_COS: /* 1332-1346 */
+        T::sincos_(x, &s, &c);
+        { R ch = T::cosh_(y), sh = T::sinh_(y); X = c * ch; Y = (-s) * sh; }
+        break;
+    case V_TAN: { /* 1351-1366 */
+        T::sincos_(R(2.0) * x, &s, &c);
+        R sh = T::sinh_(R(2.0) * y), ch = T::cosh_(R(2.0) * y);
+        d = T::recip_(c + ch);
+        X = s * d; Y = sh * d; break;
+    }
+    case V_SEC: { /* 1371-1386 */
+        T::sincos_(x, &s, &c);
+        R sh = T::sinh_(y), ch = T::cosh_(y);
+        d = T::recip_(T::cos_(R(2.0) * x) + T::cosh_(R(2.0) * y));
+        X = (c * ch) * d; Y = (s * sh) * d; break;
+    }
+    case V_CSC: { /* 1391-1406 */
+        T::sincos_(x, &s, &c);
+        R sh = T::sinh_(y), ch = T::cosh_(y);
+        d = T::recip_(T::cosh_(R(2.0) * y) - T::cos_(R(2.0) * x));
+        X = (s * ch) * d; Y = ((-c) * sh) * d; break;
+    }
+    case V_COT: { /* 1411-1426 */
+        T::sincos_(R(2.0) * x, &s, &c);
+        R sh = T::sinh_(R(2.0) * y), ch = T::cosh_(R(2.0) * y);
+        d = T::recip_(ch - c);
+        X = s * d; Y = (-sh) * d; break;
+    }
+    case V_SINH: { /* 1431-1445 */
+        T::sincos_(y, &s, &c);
+        R sh = T::sinh_(x), ch = T::cosh_(x);
+        X = sh * c; Y = ch * s; break;
+    }
+    case V_COSH: { /* 1450-1464 */
+        T::sincos_(y, &s, &c);
+        R sh = T::sinh_(x), ch = T::cosh_(x);
+        X = ch * c; Y = sh * s; break;
+    }
+    case V_TANH: { /* 1469-1484 */
+        T::sincos_(R(2.0) * y, &s, &c);
+        R sh = T::sinh_(R(2.0) * x), ch = T::cosh_(R(2.0) * x);
+        d = T::recip_(c + ch);
+        X = sh * d; Y = s * d; break;
+    }
+    case V_SECH: { /* 1489-1504 */
+        T::sincos_(y, &s, &c);
+        R sh = T::sinh_(x), ch = T::cosh_(x);
+        d = T::recip_(T::cos_(R(2.0) * y) + T::cosh_(R(2.0) * x));
+        X = (c * ch) * d; Y = ((-s) * sh) * d; break;
+    }
+    case V_CSCH: { /* 1509-1524 */
+        T::sincos_(y, &s, &c);
+        R sh = T::sinh_(x), ch = T::cosh_(x);
+        d = T::recip_(T::cosh_(R(2.0) * x) - T::cos_(R(2.0) * y));
+        X = (sh * c) * d; Y = ((-ch) * s) * d; break;
+    }
+    case V_COTH: { /* 1529-1544 */
+        T::sincos_(R(2.0) * y, &s, &c);
+        R sh = T::sinh_(R(2.0) * x), ch = T::cosh_(R(2.0) * x);
+        d = T::recip_(ch - c);
+        X = sh * d; Y = s * d; break;
+    }
+    case V_AUGER: { /* 1549-1571: p = freq, weight, scale/2, sym */
+        R ss = T::sin_(P[0] * x), tt = T::sin_(P[0] * y);
+        R dy = y + P[1] * (P[2] + T::fabs_(y)) * ss;
+        R dx = x + P[1] * (P[2] + T::fabs_(x)) * tt;
+        X = x + P[3] * (dx - x); Y = dy; break;
+    }
+    case V_FLUX: { /* 1576-1600: p = 2 + spread, weight */
+        R xpw = x + P[1], xmw = x - P[1], y2 = y * y;
+        R avgr = P[0] * T::sqrt_(T::sqrt_(y2 + xpw * xpw) / T::sqrt_(y2 + xmw * xmw));
+        R avga = (T::atan2_(y, xmw) - T::atan2_(y, xpw)) * R(0.5);
+        /* sincosg(avga, c, s) stores the sine in c (variations.hpp:1597) */
+        T::sincos_(avga, &c, &s);
+        X = c * avgr; Y = s * avgr; break;
+    }
+    case V_MOBIUS: { /* 1605-1630: p = a0 a1 b0 b1 c0 c1 d0 d1 */
+        R re_u = P[0] * x - P[1] * y + P[2];
+        R im_u = P[0] * y + P[1] * x + P[3];
+        R re_v = P[4] * x - P[5] * y + P[6];
+        R im_v = P[4] * y + P[5] * x + P[7];
+        R rad = T::recip_(re_v * re_v + im_v * im_v + T::eps);
+        X = (re_u * re_v + im_u * im_v) * rad;
+        Y = (im_u * re_v - re_u * im_v) * rad; break;
+    }
+    case V_SCRY: { /* 1635-1650 */
+        R tt = R2SQ;
+        r = T::recip_(T::sqrt_(tt) * (tt + T::recip_(P[0] + T::eps)));
+        X = x * r; Y = y * r; break;
+    }
+    case V_SPLIT: { /* 1655-1673: p = xsize*pi, ysize*pi */
+        R xs = T::copysign_(R(1.0), T::cos_(x * P[0]));
+        R ys = T::copysign_(R(1.0), T::cos_(y * P[1]));
+        X = x * ys; Y = y * xs; break;
+    }
+    case V_STRIPES: { /* 1678-1696: p = 1 - space, warp */
+        R rx = T::floor_(x + R(0.5)), ox = x - rx;
+        X = ox * P[0] + rx; Y = y + ox * ox * P[1]; break;
+    }
+    case V_WEDGE: { /* 1701-1724: p = swirl, count, angle, hole, cf */
+        r = R2;
+        a = T::atan2_(y, x) + P[0] * r;
+        R cc = T::floor_((P[1] * a + T::pi) * (T::inv_pi * R(0.5)));
+        a = a * P[4] + cc * P[2];
+        T::sincos_(a, &s, &c);
+        X = c * (r + P[3]); Y = s * (r + P[3]); break;
+    }
+    case V_WEDGE_JULIA: { /* 1729-1756: p = angle, count, invpower, cn, abspower, cf */
+        r = T::pow_(R2SQ, P[3]);
+        int32_t tr = (int32_t)(P[4] * T::unit(rng.next()));
+        a = (T::atan2_(y, x) + (R(2.0) * T::pi) * tr) * P[2];
+        R cc = T::floor_((P[1] * a + T::pi) * (T::inv_pi * R(0.5)));
+        a = a * P[5] + cc * P[0];
+        T::sincos_(a, &s, &c);
+        X = c * r; Y = s * r; break;
+    }
+    case V_WEDGE_SPH: { /* 1761-1785: p = angle, count, swirl, hole, cf */
+        r = T::recip_(R2 + T::eps);
+        a = T::atan2_(y, x) + P[2] * r;
+        R cc = T::floor_((P[1] * a + T::pi) * (T::inv_pi * R(0.5)));
+        a = a * P[4] + cc * P[0];
+        T::sincos_(a, &s, &c);
+        X = c * (r + P[3]); Y = s * (r + P[3]); break;
+    }
+    case V_WHORL: /* 1790-1810: p = inside, outside, weight */
+        r = R2;
+        a = T::atan2_(y, x);
+        a += (r >= P[2] ? P[1] : P[0]) / (P[2] - r);
+        T::sincos_(a, &s, &c);
+        X = c * r; Y = s * r; break;
+    case V_SUPERSHAPE: { /* 1815-1842: p = m/4, -1/n1, n2, n3, rnd, holes */
+        R theta = P[0] * T::atan2_(y, x) + T::pi_4;
+        R st, ct;
+        T::sincos_(theta, &st, &ct);
+        R t1 = T::pow_(T::fabs_(ct), P[2]), t2 = T::pow_(T::fabs_(st), P[3]);
+        R tr = R2;
+        r = (P[4] * T::unit(rng.next()) + (R(1.0) - P[4]) * tr) - P[5];
+        r *= T::pow_(t1 + t2, P[1]) / tr;
+        X = x * r; Y = y * r; break;
+    }
+    case V_FLOWER: /* 1847-1864: p = petals, holes */
+        r = (T::unit(rng.next()) - P[1]) * T::cos_(P[0] * T::atan2_(y, x));
+        r /= R2 + T::eps;
+        X = x * r; Y = y * r; break;
+    case V_CONIC: { /* 1869-1886: p = eccen, holes */
+        R tr = R2;
+        R ct = x / (tr + T::eps);
+        r = (T::unit(rng.next()) - P[1]) * P[0] / (tr + tr * P[0] * ct);
+        X = x * r; Y = y * r; break;
+    }
+    case V_PARABOLA: { /* 1891-1909: p = height, width */
+        R sr, cr;
+        T::sincos_(R2, &sr, &cr);
+        X = P[0] * sr * sr * T::unit(rng.next());
+        Y = P[1] * cr * T::unit(rng.next()); break;
+    }
+    case V_BIPOLAR: { /* 1914-1935: p = -pi/2 * shift */
+        R x2y2 = R2SQ, tt = x2y2 + R(1.0), x2 = R(2.0) * x;
+        R yy = R(0.5) * T::atan2_(R(2.0) * y, x2y2 - R(1.0)) + P[0];
+        yy -= T::pi * T::floor_(yy * T::inv_pi + R(0.5));
+        X = T::log_((tt + x2) / (tt - x2)); Y = yy; break;
+    }
+    case V_BOARDERS: { /* 1940-1983: p = prob */
+        R rx = T::rint_(x), ry = T::rint_(y), ox = x - rx, oy = y - ry;
+        if (T::unit(rng.next()) >= P[0]) {
+            X = ox * R(0.5) + rx; Y = oy * R(0.5) + ry;
+        } else {
+            R mag = R(1.0) - P[0];
+            if (T::fabs_(ox) >= T::fabs_(oy)) {
+                R sg = T::copysign_(mag, ox);
+                X = ox * R(0.5) + rx + sg; Y = oy * R(0.5) + ry + sg * oy / ox;
+            } else {
+                R sg = T::copysign_(mag, oy);
+                X = ox * R(0.5) + rx + sg * ox / oy; Y = oy * R(0.5) + ry + sg;
+            }
+        }
         break;
     }
-    default:
-        // unreachable: the host rejects variations this build lacks
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-            o[i] = R(0) / R(0);
-        return;
+    case V_BUTTERFLY: { /* 1988-2003 */
+        R y2 = R(2.0) * y;
+        r = T::sqrt_(T::fabs_(x * y) / (x * x + y2 * y2 + T::eps));
+        X = x * r; Y = y2 * r; break;
     }
-    // 2-D result into the (axis_x, axis_y) plane, zero elsewhere
-#pragma unroll
+    case V_CELL: { /* 2008-2033: p = size, 1/size */
+        R fx = T::floor_(x * P[1]), fy = T::floor_(y * P[1]);
+        R dx = x - fx * P[0], dy = y - fy * P[0];
+        R xs = T::copysign_(R(2.0), fx), ys = T::copysign_(R(2.0), fy);
+        R x2 = fx * xs, y2 = fy * ys;
+        x2 -= (R)(fx < 0);
+        y2 -= (R)(fy < 0);
+        X = dx + x2 * P[0]; Y = -dy - y2 * P[0]; break;
+    }
+    case V_CPOW: { /* 2038-2061: p = va, vc, vd, power */
+        a = T::atan2_(y, x);
+        R lnr = R(0.5) * T::log_(R2SQ);
+        R ang = P[1] * a + P[2] * lnr + P[0] * T::floor_(P[3] * T::unit(rng.next()));
+        T::sincos_(ang, &s, &c);
+        d = T::exp_(P[1] * lnr - P[2] * a);
+        X = c * d; Y = s * d; break;
+    }
+    case V_CURVE: /* 2066-2091: p = xamp, yamp, 1/xlen^2, 1/ylen^2 */
+        X = x + P[0] * T::exp_(-y * y * P[2]);
+        Y = y + P[1] * T::exp_(-x * x * P[3]); break;
+    case V_EDISC: { /* 2096-2120 */
+        R tmp = R2SQ + R(1.0), tmp2 = R(2.0) * x;
+        R xmax = R(0.5) * (T::sqrt_(tmp + tmp2) + T::sqrt_(tmp - tmp2));
+        R a1 = T::log_(xmax + T::sqrt_(xmax - R(1.0)));
+        R a2 = -T::acos_(x / xmax);
+        R s1, c1;
+        T::sincos_(a1, &s1, &c1);
+        R s2 = T::sinh_(a2), c2 = T::cosh_(a2);
+        s1 *= T::copysign_(R(1.0), -y);
+        X = c2 * c1; Y = s2 * s1; break;
+    }
+    case V_ELLIPTIC: { /* 2125-2144 */
+        R tmp = R2SQ + R(1.0), x2 = R(2.0) * x;
+        R xmax = R(0.5) * (T::sqrt_(tmp + x2) + T::sqrt_(tmp - x2));
+        R aa = x / xmax, bb = R(1.0) - aa * aa, ssx = xmax - R(1.0);
+        bb = bb < R(0.0) ? R(0.0) : T::sqrt_(bb);
+        ssx = ssx < R(0.0) ? R(0.0) : T::sqrt_(ssx);
+        X = T::atan2_(aa, bb); Y = T::copysign_(R(1.0), y) * T::log_(xmax + ssx); break;
+    }
+    case V_ESCHER: { /* 2149-2171: p = vc, vd */
+        a = T::atan2_(y, x);
+        R lnr = R(0.5) * T::log_(R2SQ);
+        R n = P[0] * a + P[1] * lnr;
+        T::sincos_(n, &s, &c);
+        d = T::exp_(P[0] * lnr - P[1] * a);
+        X = c * d; Y = s * d; break;
+    }
+    case V_FOCI: { /* 2176-2192 */
+        R expx = R(0.5) * T::exp_(x), expnx = R(0.25) / expx;
+        T::sincos_(y, &s, &c);
+        d = T::recip_(expx + expnx - c);
+        X = (expx - expnx) * d; Y = s * d; break;
+    }
+    case V_LAZYSUSAN: { /* 2197-2230: p = x, y, spin, twist, space, weight */
+        R xx = x - P[0], yy = y + P[1];
+        r = T::hypot_(xx, yy);
+        if (r < P[5]) {
+            a = T::atan2_(yy, xx) + P[2] + P[3] * (P[5] - r);
+            T::sincos_(a, &s, &c);
+            X = r * c + P[0]; Y = r * s - P[1];
+        } else {
+            r = R(1.0) + P[4] / (r + T::eps);
+            X = r * xx + P[0]; Y = r * yy - P[1];
+        }
+        break;
+    }
+    case V_LOONIE: { /* 2235-2254: p = weight, weight^2 */
+        R r2 = R2SQ;
+        r = P[0];
+        if (r2 < P[1])
+            r *= T::sqrt_(P[1] / (r2 + T::eps) - R(1.0));
+        X = x * r; Y = y * r; break;
+    }
+    case V_OSCOPE: { /* 2259-2281: p = 2 pi freq, amp, damp, sep */
+        R damp = T::exp_(-T::fabs_(x) * P[2]);
+        R tt = P[1] * damp * T::cos_(P[0] * x) + P[3];
+        X = x; Y = T::copysign_(R(1.0), T::fabs_(y) - tt) * y; break;
+    }
+    case V_POPCORN: /* 2286-2305: p = x, y, c */
+        X = x + P[0] * T::sin_(T::tan_(y * P[2]));
+        Y = y + P[1] * T::sin_(T::tan_(x * P[2])); break;
+    default:
+        X = Y = (R(0) / R(0)); break;
+    }
+#undef R2SQ
+#undef R2
+#undef ANG
     for (int i = 0; i < D; ++i)
-        o[i] = i == ax ? x2 : (i == ay ? y2 : R(0));
+        out[i] = i == ax ? X : (i == ay ? Y : R(0));
 }
 
 } // namespace ffr

@@ -18,10 +18,103 @@ enum {
     OR_V_LINEAR = 0,
     OR_V_SINUSOIDAL = 1,
     OR_V_SPHERICAL = 2,
+    OR_V_BENT = 3,
+    OR_V_RECTANGLES = 4,
+    OR_V_FISHEYE = 5,
+    OR_V_BUBBLE = 6,
+    OR_V_NOISE = 7,
+    OR_V_BLUR = 8,
+    OR_V_GAUSSIAN_BLUR = 9,
+    OR_V_SQUARE_NOISE = 10,
+    OR_V_SEPARATION = 11,
+    OR_V_SPLITS = 12,
+    OR_V_PRE_BLUR = 13,
+    OR_V_MODULUS = 14,
+    OR_V_CELLN = 15,
+    OR_V_SPHERICAL_P = 16,
+    OR_V_UNIT_SPHERE = 17,
+    OR_V_UNIT_SPHERE_P = 18,
+    OR_V_UNIT_CUBE = 19,
     OR_V_SWIRL = 20,
     OR_V_HORSESHOE = 21,
     OR_V_POLAR = 22,
-    OR_V_JULIA = 35
+    OR_V_POLAR2 = 23,
+    OR_V_HANDKERCHIEF = 24,
+    OR_V_HEART = 25,
+    OR_V_DISC = 26,
+    OR_V_DISC2 = 27,
+    OR_V_WAVES = 28,
+    OR_V_FAN = 29,
+    OR_V_RINGS = 30,
+    OR_V_SPIRAL = 31,
+    OR_V_HYPERBOLIC = 32,
+    OR_V_DIAMOND = 33,
+    OR_V_EX = 34,
+    OR_V_JULIA = 35,
+    OR_V_EXPONENTIAL = 36,
+    OR_V_POWER = 37,
+    OR_V_COSINE = 38,
+    OR_V_BLOB = 39,
+    OR_V_PDJ = 40,
+    OR_V_CYLINDER = 41,
+    OR_V_PERSPECTIVE = 42,
+    OR_V_JULIAN = 43,
+    OR_V_JULIASCOPE = 44,
+    OR_V_RADIAL_BLUR = 45,
+    OR_V_PIE = 46,
+    OR_V_NGON = 47,
+    OR_V_CURL = 48,
+    OR_V_ARCH = 49,
+    OR_V_TANGENT = 50,
+    OR_V_RAYS = 51,
+    OR_V_BLADE = 52,
+    OR_V_SECANT = 53,
+    OR_V_TWINTRIAN = 54,
+    OR_V_CROSS = 55,
+    OR_V_EXP = 56,
+    OR_V_LOG = 57,
+    OR_V_SIN = 58,
+    OR_V_COS = 59,
+    OR_V_TAN = 60,
+    OR_V_SEC = 61,
+    OR_V_CSC = 62,
+    OR_V_COT = 63,
+    OR_V_SINH = 64,
+    OR_V_COSH = 65,
+    OR_V_TANH = 66,
+    OR_V_SECH = 67,
+    OR_V_CSCH = 68,
+    OR_V_COTH = 69,
+    OR_V_AUGER = 70,
+    OR_V_FLUX = 71,
+    OR_V_MOBIUS = 72,
+    OR_V_SCRY = 73,
+    OR_V_SPLIT = 74,
+    OR_V_STRIPES = 75,
+    OR_V_WEDGE = 76,
+    OR_V_WEDGE_JULIA = 77,
+    OR_V_WEDGE_SPH = 78,
+    OR_V_WHORL = 79,
+    OR_V_SUPERSHAPE = 80,
+    OR_V_FLOWER = 81,
+    OR_V_CONIC = 82,
+    OR_V_PARABOLA = 83,
+    OR_V_BIPOLAR = 84,
+    OR_V_BOARDERS = 85,
+    OR_V_BUTTERFLY = 86,
+    OR_V_CELL = 87,
+    OR_V_CPOW = 88,
+    OR_V_CURVE = 89,
+    OR_V_EDISC = 90,
+    OR_V_ELLIPTIC = 91,
+    OR_V_ESCHER = 92,
+    OR_V_FOCI = 93,
+    OR_V_LAZYSUSAN = 94,
+    OR_V_LOONIE = 95,
+    OR_V_OSCOPE = 96,
+    OR_V_POPCORN = 97,
+    OR_V_COUNT = 98,
+    OR_FIRST_2D = 20
 };
 
 typedef struct {
@@ -74,6 +167,7 @@ int oracle_step(const or_flame *f, int xf_index, uint64_t key, uint64_t npts,
 int oracle_render(const or_flame *f, uint64_t seed, uint64_t streams,
     uint64_t samples, uint64_t traj_len, uint64_t settle, uint64_t bad_limit,
     int threads, uint64_t *counts, double *colors, or_stats *out);
+int oracle_variation_words(int type, int dims);
 int oracle_trace(const or_flame *f, uint64_t key, uint64_t settle, uint64_t n,
     int32_t *ids, double *pts);
 

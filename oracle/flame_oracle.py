@@ -70,11 +70,209 @@ TWO_D_NAMES = [
 ALL_NAMES = ND_NAMES + TWO_D_NAMES
 VAR_ID = {n: i for i, n in enumerate(ALL_NAMES)}
 
-# variations implemented by this restatement -> RNG words drawn per call
-IMPLEMENTED = {
-    "linear": 0, "sinusoidal": 0, "spherical": 0, "swirl": 0,
-    "horseshoe": 0, "polar": 0, "julia": 1,
-}
+M_PI = 3.141592653589793
+M_PI_2 = 1.5707963267948966
+M_1_PI = 0.3183098861837907        # the double nearest 1/pi (glibc M_1_PI)
+EPS = 1e-20
+
+
+def _fdiv(a: float, b: float) -> float:
+    """IEEE double division (inf/nan instead of ZeroDivisionError)."""
+    with np.errstate(all="ignore"):
+        return float(np.float64(a) / np.float64(b))
+
+
+def _sin(x):
+    with np.errstate(all="ignore"):
+        return float(np.sin(np.float64(x))) if not math.isfinite(x) else math.sin(x)
+
+
+def _cos(x):
+    with np.errstate(all="ignore"):
+        return float(np.cos(np.float64(x))) if not math.isfinite(x) else math.cos(x)
+
+
+def rng_words(name: str, dims: int) -> int:
+    """RNG words one call draws (FlameRNG draw counts, flame_rng.hpp)."""
+    dw = 2 if dims == 3 else 1
+    if name in ("noise", "blur"):
+        return 1 + dw
+    if name in ("gaussian_blur", "pre_blur"):
+        return 2 + dw
+    if name == "square_noise":
+        return dims
+    if name in ("julia", "julian", "arch", "rays", "blade", "twintrian",
+                "wedge_julia", "supershape", "flower", "conic", "boarders", "cpow"):
+        return 1
+    if name in ("juliascope", "radial_blur", "parabola"):
+        return 2
+    if name == "pie":
+        return 3
+    return 0
+
+
+def _f(j, k, name):
+    return float_value(key(j, k, name), f"{name}: {k}")
+
+
+def _pt(j, k, n, name):
+    return point_value(key(j, k, name), n, f"{name}: {k}")
+
+
+def _params(name: str, j, dims: int) -> list:
+    """Constructor arithmetic of each variation class (variations.hpp)."""
+    f = lambda k: _f(j, k, name)
+    if name in ("linear", "sinusoidal", "spherical", "noise", "blur",
+                "gaussian_blur", "square_noise", "pre_blur", "unit_sphere",
+                "unit_cube"):
+        return []
+    if name == "bent":                                   # 216-240
+        return _pt(j, "scales_neg", dims, name) + _pt(j, "scales_pos", dims, name)
+    if name in ("rectangles", "splits"):                 # 245-270, 410-429
+        return _pt(j, "params", dims, name)
+    if name in ("fisheye", "bubble"):                    # 275-314
+        return [f("addval")]
+    if name == "separation":                             # 383-405
+        sep = _pt(j, "params", dims, name)
+        return [v * v for v in sep] + _pt(j, "inside", dims, name)
+    if name == "modulus":                                # 451-471
+        p2 = [v * 2.0 for v in _pt(j, "params", dims, name)]
+        return p2 + [_fdiv(1.0, v) for v in p2]
+    if name == "celln":                                  # 476-505
+        sz = _pt(j, "sizes", dims, name)
+        return sz + [_fdiv(1.0, v) for v in sz]
+    if name in ("spherical_p", "unit_sphere_p"):         # 2312-2363
+        n = f("norm")
+        if n <= 0.0:
+            raise FlameError("norm <= 0")
+        return [n]
+    if name in ("swirl", "horseshoe", "polar", "polar2", "handkerchief", "heart",
+                "disc", "spiral", "hyperbolic", "diamond", "ex", "julia",
+                "exponential", "power", "cosine", "cylinder", "tangent", "cross",
+                "exp", "log", "sin", "cos", "tan", "sec", "csc", "cot", "sinh",
+                "cosh", "tanh", "sech", "csch", "coth", "butterfly", "edisc",
+                "elliptic", "foci"):
+        return []
+    if name == "disc2":                                  # 624-655
+        rot, twist = f("rotation"), f("twist")
+        rotpi = rot * M_PI
+        sinadd, cosadd = _sin(twist), _cos(twist)
+        cosadd -= 1.0
+        k = 1.0 + twist
+        if twist > 2.0 * M_PI:
+            k -= 2.0 * M_PI
+        if twist < -2.0 * M_PI:
+            k += 2.0 * M_PI
+        return [rotpi, cosadd * k, sinadd * k]
+    if name == "waves":                                  # 660-680
+        return [f("xfreq"), f("xscale"), f("yfreq"), f("yscale")]
+    if name == "fan":                                    # 685-709
+        x, y = f("x"), f("y")
+        return [M_PI * (x * x + EPS), y]
+    if name == "rings":                                  # 714-733
+        v = f("value")
+        return [v * v + EPS]
+    if name == "blob":                                   # 875-896
+        low, high = f("low"), f("high")
+        return [(high + low) / 2.0, (high - low) / 2.0, f("waves")]
+    if name == "pdj":                                    # 901-925
+        return [f("a"), f("b"), f("c"), f("d")]
+    if name == "perspective":                            # 943-962
+        dist, ang = f("distance"), f("angle")
+        return [dist, _sin(ang), dist * _cos(ang)]
+    if name in ("julian", "juliascope"):                 # 967-1018
+        power, dist = f("power"), f("dist")
+        return [abs(power), _fdiv(1.0, power), _fdiv(dist, 2.0 * power)]
+    if name == "radial_blur":                            # 1023-1045
+        ang = f("angle")
+        a = ang * M_PI_2
+        return [_sin(a), _cos(a), f("flam3_weight")]
+    if name == "pie":                                    # 1050-1072
+        slices, rot, thick = f("slices"), f("rotation"), f("thickness")
+        return [slices, rot, thick, _fdiv(2.0 * M_PI, slices)]
+    if name == "ngon":                                   # 1077-1102
+        sides = f("sides")
+        powerval = f("power") / 2.0
+        ang = _fdiv(2.0 * M_PI, sides)
+        corners, circle = f("corners"), f("circle")
+        return [powerval, ang, corners, circle, sides / (2.0 * M_PI)]
+    if name == "curl":                                   # 1107-1129
+        return [f("c1"), f("c2")]
+    if name in ("arch", "rays", "blade", "secant", "twintrian", "scry"):
+        return [f("flam3_weight")]
+    if name == "auger":                                  # 1549-1571
+        freq, w = f("freq"), f("flam3_weight")
+        return [freq, w, f("scale") / 2.0, f("sym")]
+    if name == "flux":                                   # 1576-1600
+        return [2.0 + f("spread"), f("flam3_weight")]
+    if name == "mobius":                                 # 1605-1630
+        out = []
+        for k in ("a", "b", "c", "d"):
+            out += _pt(j, k, 2, name)
+        return out
+    if name == "split":                                  # 1655-1673
+        return [f("xsize") * M_PI, f("ysize") * M_PI]
+    if name == "stripes":                                # 1678-1696
+        return [1.0 - f("space"), f("warp")]
+    if name == "wedge":                                  # 1701-1724
+        swirl, count, ang, hole = f("swirl"), f("count"), f("angle"), f("hole")
+        return [swirl, count, ang, hole, 1.0 - ang * count * (M_1_PI * 0.5)]
+    if name == "wedge_julia":                            # 1729-1756
+        ang, count, power = f("angle"), f("count"), f("power")
+        invpower = _fdiv(1.0, power)
+        dist = f("dist")
+        cn = _fdiv(dist, 2.0 * power)
+        return [ang, count, invpower, cn, abs(power),
+                1.0 - ang * count * (M_1_PI * 0.5)]
+    if name == "wedge_sph":                              # 1761-1785
+        ang, count, swirl, hole = f("angle"), f("count"), f("swirl"), f("hole")
+        return [ang, count, swirl, hole, 1.0 - ang * count * (M_1_PI * 0.5)]
+    if name == "whorl":                                  # 1790-1810
+        return [f("inside"), f("outside"), f("flam3_weight")]
+    if name == "supershape":                             # 1815-1842
+        n1 = f("n1")
+        pm_4 = f("m") / 4.0
+        return [pm_4, _fdiv(-1.0, n1), f("n2"), f("n3"), f("rnd"), f("holes")]
+    if name == "flower":                                 # 1847-1864
+        return [f("petals"), f("holes")]
+    if name == "conic":                                  # 1869-1886
+        return [f("eccen"), f("holes")]
+    if name == "parabola":                               # 1891-1909
+        return [f("height"), f("width")]
+    if name == "bipolar":                                # 1914-1935
+        return [-M_PI_2 * f("shift")]
+    if name == "boarders":                               # 1940-1983
+        prob = f("prob")
+        if prob < 0.0 or prob > 1.0:
+            raise FlameError("boarders probability out of range")
+        return [prob]
+    if name == "cell":                                   # 2008-2033
+        size = f("size")
+        return [size, _fdiv(1.0, size)]
+    if name == "cpow":                                   # 2038-2061
+        r, i, power = f("r"), f("i"), f("power")
+        return [_fdiv(2.0 * M_PI, power), _fdiv(r, power), _fdiv(i, power), power]
+    if name == "curve":                                  # 2066-2091
+        xamp, yamp, xlen, ylen = f("xamp"), f("yamp"), f("xlen"), f("ylen")
+        xlen *= xlen
+        ylen *= ylen
+        mx = xlen if EPS < xlen else EPS
+        my = ylen if EPS < ylen else EPS
+        return [xamp, yamp, 1.0 / mx, 1.0 / my]
+    if name == "escher":                                 # 2149-2171
+        beta = f("beta")
+        return [0.5 * (1.0 + _cos(beta)), 0.5 * _sin(beta)]
+    if name == "lazysusan":                              # 2197-2230
+        return [f("x"), f("y"), f("spin"), f("twist"), f("space"), f("flam3_weight")]
+    if name == "loonie":                                 # 2235-2254
+        w = f("flam3_weight")
+        return [w, w * w]
+    if name == "oscope":                                 # 2259-2281
+        freq = f("frequency")
+        return [2.0 * M_PI * freq, f("amplitude"), f("damping"), f("separation")]
+    if name == "popcorn":                                # 2286-2305
+        return [f("x"), f("y"), f("c")]
+    raise FlameError(f"unknown variation: {name}")
 
 
 class FlameError(ValueError):
@@ -232,6 +430,7 @@ def parse_variation(j, dims: int) -> Var:
         raise FlameError(f"unknown variation: {name}")
     weight = float_value(key(j, "weight", "variation"), "variation weight")
     v = Var(name=name, weight=weight)
+    v.params = _params(name, j, dims)
     if is2d and dims > 2:
         ax = int_value(key(j, "axis_x", name), "axis_x")
         ay = int_value(key(j, "axis_y", name), "axis_y")
@@ -242,8 +441,6 @@ def parse_variation(j, dims: int) -> Var:
         if ax == ay:
             raise FlameError("axes are not distinct")
         v.axis_x, v.axis_y = ax, ay
-    if name not in IMPLEMENTED:
-        raise NotImplementedError(f"oracle: variation {name} not restated")
     return v
 
 
@@ -441,7 +638,7 @@ class OracleFlame:
             for v in x.vars:
                 cv = self._vars[vi]
                 cv.type, cv.axis_x, cv.axis_y = v.type, v.axis_x, v.axis_y
-                cv.rng_draws = IMPLEMENTED.get(v.name, 0)
+                cv.rng_draws = rng_words(v.name, n)
                 cv.weight = v.weight
                 for p, val in enumerate(v.params):
                     cv.params[p] = val

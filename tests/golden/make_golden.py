@@ -142,6 +142,121 @@ RENDERS = [
     ("julia3", 19, 8, 20000, 1000, 20, 256, "mirror"),
 ]
 
+# parameters for every variation that takes any (keys as the reference reads them)
+VAR_PARAMS = {
+    "bent": lambda d: {"scales_neg": [2.0, 0.5, 1.5][:d], "scales_pos": [1.0, 1.0, 0.8][:d]},
+    "rectangles": lambda d: {"params": [0.3, 0.5, 0.0][:d]},
+    "fisheye": lambda d: {"addval": 1.0},
+    "bubble": lambda d: {"addval": 4.0},
+    "separation": lambda d: {"params": [0.2, 0.3, 0.1][:d], "inside": [0.1, -0.2, 0.05][:d]},
+    "splits": lambda d: {"params": [0.1, 0.2, 0.15][:d]},
+    "modulus": lambda d: {"params": [0.6, 0.4, 0.5][:d]},
+    "celln": lambda d: {"sizes": [0.5, 0.7, 0.3][:d]},
+    "spherical_p": lambda d: {"norm": 1.5},
+    "unit_sphere_p": lambda d: {"norm": 3.0},
+    "disc2": lambda d: {"rotation": 0.7, "twist": 0.4},
+    "waves": lambda d: {"xfreq": 2.0, "xscale": 0.3, "yfreq": 3.0, "yscale": 0.2},
+    "fan": lambda d: {"x": 0.4, "y": 0.3},
+    "rings": lambda d: {"value": 0.6},
+    "blob": lambda d: {"low": 0.3, "high": 1.1, "waves": 5},
+    "pdj": lambda d: {"a": 1.1, "b": -1.3, "c": 0.9, "d": 1.7},
+    "perspective": lambda d: {"distance": 2.5, "angle": 0.6},
+    "julian": lambda d: {"power": 3, "dist": 1.2},
+    "juliascope": lambda d: {"power": -2.5, "dist": 0.8},
+    "radial_blur": lambda d: {"angle": 0.4, "flam3_weight": 0.5},
+    "pie": lambda d: {"slices": 6, "rotation": 0.3, "thickness": 0.5},
+    "ngon": lambda d: {"sides": 5, "power": 2.0, "corners": 0.3, "circle": 1.0},
+    "curl": lambda d: {"c1": 0.4, "c2": 0.2},
+    "arch": lambda d: {"flam3_weight": 0.7},
+    "rays": lambda d: {"flam3_weight": 0.7},
+    "blade": lambda d: {"flam3_weight": 0.7},
+    "secant": lambda d: {"flam3_weight": 0.7},
+    "twintrian": lambda d: {"flam3_weight": 0.7},
+    "scry": lambda d: {"flam3_weight": 0.7},
+    "auger": lambda d: {"freq": 2.0, "flam3_weight": 0.6, "scale": 1.0, "sym": 0.4},
+    "flux": lambda d: {"spread": 0.3, "flam3_weight": 0.4},
+    "mobius": lambda d: {"a": [0.6, 0.2], "b": [0.1, -0.3], "c": [0.3, 0.1], "d": [1.0, 0.2]},
+    "split": lambda d: {"xsize": 0.4, "ysize": 0.6},
+    "stripes": lambda d: {"space": 0.3, "warp": 0.5},
+    "wedge": lambda d: {"swirl": 0.3, "count": 3, "angle": 0.5, "hole": 0.1},
+    "wedge_julia": lambda d: {"angle": 0.4, "count": 2, "power": 3, "dist": 1.0},
+    "wedge_sph": lambda d: {"angle": 0.4, "count": 2, "swirl": 0.2, "hole": 0.05},
+    "whorl": lambda d: {"inside": 0.3, "outside": 0.5, "flam3_weight": 0.8},
+    "supershape": lambda d: {"n1": 2.0, "m": 5, "n2": 1.5, "n3": 1.5, "rnd": 0.2, "holes": 0.1},
+    "flower": lambda d: {"petals": 4, "holes": 0.2},
+    "conic": lambda d: {"eccen": 0.7, "holes": 0.1},
+    "parabola": lambda d: {"height": 0.8, "width": 1.2},
+    "bipolar": lambda d: {"shift": 0.3},
+    "boarders": lambda d: {"prob": 0.6},
+    "cell": lambda d: {"size": 0.4},
+    "cpow": lambda d: {"r": 1.2, "i": 0.3, "power": 2.5},
+    "curve": lambda d: {"xamp": 0.3, "yamp": 0.4, "xlen": 0.6, "ylen": 0.8},
+    "escher": lambda d: {"beta": 0.7},
+    "lazysusan": lambda d: {"x": 0.2, "y": -0.1, "spin": 0.5, "twist": 0.3, "space": 0.4,
+                            "flam3_weight": 0.6},
+    "loonie": lambda d: {"flam3_weight": 0.9},
+    "oscope": lambda d: {"frequency": 2.0, "amplitude": 0.5, "damping": 0.3, "separation": 0.2},
+    "popcorn": lambda d: {"x": 0.2, "y": 0.15, "c": 0.8},
+}
+
+ND_VARS = ["linear", "sinusoidal", "spherical", "bent", "rectangles", "fisheye",
+           "bubble", "noise", "blur", "gaussian_blur", "square_noise", "separation",
+           "splits", "pre_blur", "modulus", "celln", "spherical_p", "unit_sphere",
+           "unit_sphere_p", "unit_cube"]
+TWO_D_VARS = [
+    "swirl", "horseshoe", "polar", "polar2", "handkerchief", "heart", "disc",
+    "disc2", "waves", "fan", "rings", "spiral", "hyperbolic", "diamond", "ex",
+    "julia", "exponential", "power", "cosine", "blob", "pdj", "cylinder",
+    "perspective", "julian", "juliascope", "radial_blur", "pie", "ngon",
+    "curl", "arch", "tangent", "rays", "blade", "secant", "twintrian",
+    "cross", "exp", "log", "sin", "cos", "tan", "sec", "csc", "cot", "sinh",
+    "cosh", "tanh", "sech", "csch", "coth", "auger", "flux", "mobius", "scry",
+    "split", "stripes", "wedge", "wedge_julia", "wedge_sph", "whorl",
+    "supershape", "flower", "conic", "parabola", "bipolar", "boarders",
+    "butterfly", "cell", "cpow", "curve", "edisc", "elliptic", "escher",
+    "foci", "lazysusan", "loonie", "oscope", "popcorn"]
+
+
+def var_obj(name, dims, weight, axes=None):
+    v = {"name": name, "weight": weight}
+    v.update(VAR_PARAMS.get(name, lambda d: {})(dims))
+    if axes is not None:
+        v["axis_x"], v["axis_y"] = axes
+    return v
+
+
+def variation_flame(name, dims, axes=None):
+    """Two xforms: the variation under test (weight 0.7) plus linear, then a
+    plain contraction, so trajectories stay bounded."""
+    A = {1: [[0.6]], 2: [[0.6, 0.2], [-0.1, 0.7]],
+         3: [[0.6, 0.2, 0.0], [-0.1, 0.7, 0.1], [0.05, 0.0, 0.65]]}[dims]
+    b = [0.1, -0.05, 0.03][:dims]
+    I5 = [[0.5 if i == k else 0.0 for k in range(dims)] for i in range(dims)]
+    return {
+        "dimensions": dims, "size": [32] * dims if dims < 3 else [16] * 3,
+        "bounds": [[-2.0, 2.0]] * dims,
+        "xforms": [
+            {"weight": 1.0, "pre_affine": {"A": A, "b": b},
+             "variations": [var_obj(name, dims, 0.7, axes),
+                            {"name": "linear", "weight": 0.3}]},
+            {"weight": 0.5, "pre_affine": {"A": I5, "b": [-0.3, 0.2, 0.1][:dims]},
+             "variations": [{"name": "linear", "weight": 1.0}]},
+        ]}
+
+
+def variation_set():
+    out = {}
+    for n in ND_VARS:
+        for d in (1, 2, 3):
+            out[f"v{d}_{n}"] = variation_flame(n, d)
+    for n in TWO_D_VARS:
+        out[f"v2_{n}"] = variation_flame(n, 2)
+    for k, n in enumerate(TWO_D_VARS):
+        if k % 3 == 0:
+            out[f"v3_{n}"] = variation_flame(n, 3, axes=(2, 0) if k % 2 else (1, 2))
+    return out
+
+
 INVALID = {
     "no_xforms": '{"dimensions":2,"size":[4,4],"bounds":[[0,1],[0,1]],"xforms":[]}',
     "all_zero": '{"dimensions":2,"size":[4,4],"bounds":[[0,1],[0,1]],"xforms":[{"weight":0,"variations":[]}]}',
@@ -266,6 +381,37 @@ def main():
                                stderr=subprocess.PIPE, text=True)
         manifest["valid_edge"][name] = {"text": text, "ok": r.returncode == 0,
                                         "dump": json.loads(r.stdout) if r.returncode == 0 else None}
+    # every variation: flame, single steps, a trace and a small render
+    manifest["vflames"] = {}
+    vdir = os.path.join(FLAMES, "var")
+    ddir = os.path.join(DATA, "var")
+    os.makedirs(vdir, exist_ok=True)
+    os.makedirs(ddir, exist_ok=True)
+    vrng = np.random.Generator(np.random.PCG64(4242))
+    for name, fl in variation_set().items():
+        path = os.path.join(vdir, name + ".json")
+        with open(path, "w") as f:
+            json.dump(fl, f)
+        dims = fl["dimensions"]
+        arrays = {}
+        pts = vrng.uniform(-1.5, 1.5, size=(128, dims))
+        arrays["step_in"] = pts
+        with tempfile.TemporaryDirectory() as td:
+            pin = os.path.join(td, "in.bin")
+            pout = os.path.join(td, "out.bin")
+            pts.astype(np.float64).tofile(pin)
+            ref("step", path, 0, 777, pin, pout)
+            arrays["step_out"] = np.fromfile(pout, dtype=np.float64).reshape(-1, dims)
+            lines = ref("trace", path, 999, 20, 100).strip().split("\n")
+            arrays["trace_ids"] = np.array([int(l.split()[0]) for l in lines], dtype=np.int32)
+            arrays["trace_pts"] = np.array([[hexd("0x" + h) for h in l.split()[1:]]
+                                            for l in lines])
+            out = os.path.join(td, "o.buf")
+            st = json.loads(ref("render", path, 21, 8, 20000, 1000, 20, 10**9, out))
+            arrays["counts"] = np.fromfile(out, dtype=np.uint64)
+        np.savez_compressed(os.path.join(ddir, name + ".npz"), **arrays)
+        manifest["vflames"][name] = {"dims": dims, "stats": st,
+                                     "render": [21, 8, 20000, 1000, 20, 10**9]}
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     print("golden fixtures written", file=sys.stderr)
