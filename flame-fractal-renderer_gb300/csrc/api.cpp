@@ -72,6 +72,8 @@ typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
 typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
 typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
 typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
+typedef cudaError_t (*BatchFn)(const BatchArgs&, int, int, size_t, cudaStream_t);
+typedef cudaError_t (*OccBatchFn)(int, int*, int*, size_t);
 
 struct Launchers
 {
@@ -79,6 +81,8 @@ struct Launchers
     OccFn occ;
     RenderFn sorted;
     OccSortedFn occ_sorted;
+    BatchFn batch;
+    OccBatchFn occ_batch;
     StepFn step;
     TraceFn trace;
 };
@@ -86,19 +90,25 @@ struct Launchers
 const Launchers kLaunchers[2][3] = {
     {
         {launch_render_p0_d1, occupancy_p0_d1, launch_sorted_p0_d1,
-         occupancy_sorted_p0_d1, launch_step_p0_d1, launch_trace_p0_d1},
+         occupancy_sorted_p0_d1, launch_batch_p0_d1, occupancy_batch_p0_d1,
+         launch_step_p0_d1, launch_trace_p0_d1},
         {launch_render_p0_d2, occupancy_p0_d2, launch_sorted_p0_d2,
-         occupancy_sorted_p0_d2, launch_step_p0_d2, launch_trace_p0_d2},
+         occupancy_sorted_p0_d2, launch_batch_p0_d2, occupancy_batch_p0_d2,
+         launch_step_p0_d2, launch_trace_p0_d2},
         {launch_render_p0_d3, occupancy_p0_d3, launch_sorted_p0_d3,
-         occupancy_sorted_p0_d3, launch_step_p0_d3, launch_trace_p0_d3},
+         occupancy_sorted_p0_d3, launch_batch_p0_d3, occupancy_batch_p0_d3,
+         launch_step_p0_d3, launch_trace_p0_d3},
     },
     {
         {launch_render_p1_d1, occupancy_p1_d1, launch_sorted_p1_d1,
-         occupancy_sorted_p1_d1, launch_step_p1_d1, launch_trace_p1_d1},
+         occupancy_sorted_p1_d1, launch_batch_p1_d1, occupancy_batch_p1_d1,
+         launch_step_p1_d1, launch_trace_p1_d1},
         {launch_render_p1_d2, occupancy_p1_d2, launch_sorted_p1_d2,
-         occupancy_sorted_p1_d2, launch_step_p1_d2, launch_trace_p1_d2},
+         occupancy_sorted_p1_d2, launch_batch_p1_d2, occupancy_batch_p1_d2,
+         launch_step_p1_d2, launch_trace_p1_d2},
         {launch_render_p1_d3, occupancy_p1_d3, launch_sorted_p1_d3,
-         occupancy_sorted_p1_d3, launch_step_p1_d3, launch_trace_p1_d3},
+         occupancy_sorted_p1_d3, launch_batch_p1_d3, occupancy_batch_p1_d3,
+         launch_step_p1_d3, launch_trace_p1_d3},
     },
 };
 
@@ -367,6 +377,63 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
     a.rng_words = program_words(c);
     a.agg = agg;
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+}
+
+// the leading fields of DevStats (everything before xf_dist)
+struct StatsHeadCopy
+{
+    unsigned long long s_iter, s_plot, bad_total, dropped, bad_claim;
+    unsigned int stop, cancelled;
+    unsigned long long ext_lo[kMaxDims], ext_hi[kMaxDims];
+};
+static_assert(sizeof(StatsHeadCopy) == offsetof(DevStats, xf_dist), "DevStats head layout");
+static_assert(offsetof(StatsHeadCopy, ext_lo) == offsetof(DevStats, ext_lo), "DevStats head layout");
+
+// per-xform counts (sorted order -> JSON ids) and bad-value records of the
+// last render of c into *st (the reference's stats getters)
+ffr_status read_stats(ffr_ctx* c, const StatsHeadCopy& hs, ffr_stats* st)
+{
+    std::memset(st, 0, sizeof *st);
+    for (int i = 0; i < FFR_MAX_DIMS; ++i)
+    {
+        st->ext_lo[i] = INFINITY;
+        st->ext_hi[i] = -INFINITY;
+    }
+    st->xform_ids = c->flame.xform_ids;
+    st->settle = c->opts.settle;
+    st->samples_iterated = hs.s_iter;
+    st->samples_plotted = hs.s_plot;
+    st->bad_values = hs.bad_total;
+    st->dropped = hs.dropped;
+    for (int i = 0; i < c->flame.dims; ++i)
+    {
+        st->ext_lo[i] = key_to_double(hs.ext_lo[i]);
+        st->ext_hi[i] = key_to_double(hs.ext_hi[i]);
+    }
+    const size_t nxf = c->flame.xforms.size();
+    std::vector<unsigned long long> dist(nxf);
+    CU(c, cudaMemcpy(dist.data(), c->d_stats->xf_dist, sizeof(unsigned long long) * nxf,
+                     cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < nxf; ++k)
+    {
+        const uint64_t id = c->flame.xforms[k].id;
+        if (id < FFR_MAX_XFORM_IDS)
+            st->xf_dist[id] += dist[k];
+    }
+    const unsigned long long nrec = std::min<unsigned long long>(hs.bad_claim, kMaxBadRecords);
+    if (nrec)
+    {
+        CU(c, cudaMemcpy(st->bad_xf, c->d_stats->bad_xf, sizeof(unsigned long long) * nrec,
+                         cudaMemcpyDeviceToHost));
+        std::vector<double> pts(kMaxDims * nrec);
+        CU(c, cudaMemcpy(pts.data(), c->d_stats->bad_pts, sizeof(double) * kMaxDims * nrec,
+                         cudaMemcpyDeviceToHost));
+        for (unsigned long long k = 0; k < nrec; ++k)
+            for (int i = 0; i < c->flame.dims; ++i)
+                st->bad_pts[k][i] = pts[k * kMaxDims + i];
+    }
+    st->bad_recorded = nrec;
+    return FFR_OK;
 }
 
 // Renders this large are autotuned; smaller ones use the static choice.
@@ -785,59 +852,23 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     c->count_bound += samples;
     if (s != FFR_OK)
         return s;
-    DevStats* hs = new (std::nothrow) DevStats;
-    if (!hs)
-        return fail(c, FFR_ERR_OOM, "out of host memory");
-    CU(c, cudaMemcpy(hs, c->d_stats, offsetof(DevStats, xf_dist), cudaMemcpyDeviceToHost));
-    const size_t nxf = c->flame.xforms.size();
-    CU(c, cudaMemcpy(hs->xf_dist, c->d_stats->xf_dist, sizeof(unsigned long long) * nxf,
-                     cudaMemcpyDeviceToHost));
-    const unsigned long long nrec = std::min<unsigned long long>(hs->bad_claim, kMaxBadRecords);
-    if (nrec)
-    {
-        CU(c, cudaMemcpy(hs->bad_xf, c->d_stats->bad_xf, sizeof(unsigned long long) * nrec,
-                         cudaMemcpyDeviceToHost));
-        CU(c, cudaMemcpy(hs->bad_pts, c->d_stats->bad_pts, sizeof(double) * kMaxDims * nrec,
-                         cudaMemcpyDeviceToHost));
-    }
+    StatsHeadCopy hs;
+    CU(c, cudaMemcpy(&hs, c->d_stats, sizeof hs, cudaMemcpyDeviceToHost));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    const bool failed = hs->stop != 0;
     if (st)
     {
-        st->samples_iterated = hs->s_iter;
-        st->samples_plotted = hs->s_plot;
-        st->bad_values = hs->bad_total;
-        st->dropped = hs->dropped;
-        for (int i = 0; i < c->flame.dims; ++i)
-        {
-            st->ext_lo[i] = key_to_double(hs->ext_lo[i]);
-            st->ext_hi[i] = key_to_double(hs->ext_hi[i]);
-        }
-        for (size_t k = 0; k < nxf; ++k)
-        {
-            const uint64_t id = c->flame.xforms[k].id;
-            if (id < FFR_MAX_XFORM_IDS)
-                st->xf_dist[id] += hs->xf_dist[k];
-        }
-        st->bad_recorded = nrec;
-        for (unsigned long long k = 0; k < nrec; ++k)
-        {
-            st->bad_xf[k] = hs->bad_xf[k];
-            for (int i = 0; i < c->flame.dims; ++i)
-                st->bad_pts[k][i] = hs->bad_pts[k][i];
-        }
+        if ((s = read_stats(c, hs, st)) != FFR_OK)
+            return s;
         st->streams = S;
         st->traj_len = L;
         st->kernel_ms = ms;
         st->kernel = kernel;
         st->agg = agg;
     }
-    const bool cancelled = hs->cancelled != 0;
-    delete hs;
-    if (cancelled)
+    if (hs.cancelled)
         return fail(c, FFR_ERR_TIMEOUT, "render cancelled");
-    if (failed)
+    if (hs.stop)
         return fail(c, FFR_BAD_VALUES, "render failure (flame may not be sufficiently contractive)");
     return FFR_OK;
 }
@@ -1018,6 +1049,262 @@ ffr_status ffr_trace(ffr_ctx* c, uint64_t key, uint64_t settle, uint64_t n,
     CU(c, cudaMemcpyAsync(pts, dp, pbytes, cudaMemcpyDeviceToHost, c->stream));
     CU(c, cudaMemcpyAsync(ids, di, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
     return wait_stream(c);
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------ batch
+struct ffr_batch
+{
+    std::vector<ffr_ctx*> ctxs;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    struct Group
+    {
+        int dims = 0, color = 0;
+        std::vector<int> members;
+        JobDesc* d_jobs = nullptr;          // njobs JobDesc + BatchHead
+        BatchHead* d_head = nullptr;
+        JobDesc* h_jobs = nullptr;          // pinned staging
+        size_t smem = 0;
+        int grid = 0;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::vector<Group> groups;
+    uint64_t traj_len = 4096;               // samples per stream when not set per context
+    std::string err = "no error";
+};
+
+namespace {
+
+ffr_status bfail(ffr_batch* b, ffr_status s, const std::string& m)
+{
+    b->err = m;
+    return s;
+}
+
+#define BCU(b, call)                                                   \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess)                                         \
+            return bfail((b), FFR_ERR_CUDA, std::string(#call) + ": "  \
+                         + cudaGetErrorString(e_));                    \
+    } while (0)
+
+void batch_free(ffr_batch* b)
+{
+    if (!b)
+        return;
+    cudaSetDevice(b->device);
+    if (b->stream)
+        cudaStreamSynchronize(b->stream);
+    for (auto& g : b->groups)
+    {
+        if (g.exec)
+            cudaGraphExecDestroy(g.exec);
+        cudaFree(g.d_jobs);
+        if (g.h_jobs)
+            cudaFreeHost(g.h_jobs);
+    }
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream)
+        cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+} // namespace
+
+extern "C" {
+
+ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
+{
+    if (!out || !ctxs || n == 0)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_batch_create: no contexts");
+    *out = nullptr;
+    const int dev = ctxs[0]->device, prec = ctxs[0]->opts.precision;
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (!ctxs[i])
+            return fail(nullptr, FFR_ERR_ARG, "ffr_batch_create: NULL context");
+        if (ctxs[i]->device != dev || ctxs[i]->opts.precision != prec)
+            return fail(nullptr, FFR_ERR_ARG,
+                        "ffr_batch_create: contexts must share device and precision");
+    }
+    ffr_batch* b = new (std::nothrow) ffr_batch;
+    if (!b)
+        return fail(nullptr, FFR_ERR_OOM, "out of host memory");
+    b->ctxs.assign(ctxs, ctxs + n);
+    b->device = dev;
+    cudaError_t e;
+    auto cfail = [&](cudaError_t er, const char* what) {
+        std::string m = std::string(what) + ": " + cudaGetErrorString(er);
+        batch_free(b);
+        return fail(nullptr, FFR_ERR_CUDA, m);
+    };
+    if ((e = cudaSetDevice(dev)) != cudaSuccess)
+        return cfail(e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cfail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess)
+        return cfail(e, "cudaEventCreate");
+    // group by (dims, colour): one persistent kernel instantiation each
+    for (size_t i = 0; i < n; ++i)
+    {
+        const int d = ctxs[i]->flame.dims, col = ctxs[i]->flame.color_dims > 0;
+        ffr_batch::Group* g = nullptr;
+        for (auto& x : b->groups)
+            if (x.dims == d && x.color == col)
+                g = &x;
+        if (!g)
+        {
+            b->groups.emplace_back();
+            g = &b->groups.back();
+            g->dims = d;
+            g->color = col;
+        }
+        g->members.push_back((int)i);
+    }
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (auto& g : b->groups)
+    {
+        const size_t nj = g.members.size();
+        const Launchers& L = kLaunchers[prec][g.dims - 1];
+        int bps = 0, block = 0;
+        for (int m : g.members)
+        {
+            ffr_ctx* c = ctxs[m];
+            size_t sm = 0;
+            if ((e = L.occ(g.color, 0, &bps, &block, (unsigned int)c->prog_host.size(),
+                           (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
+                return cfail(e, "occupancy");
+            g.smem = std::max(g.smem, sm);
+        }
+        if ((e = L.occ_batch(g.color, &bps, &block, g.smem)) != cudaSuccess)
+            return cfail(e, "batch occupancy");
+        if (bps < 1)
+        {
+            batch_free(b);
+            return fail(nullptr, FFR_ERR_ARG, "batched kernel does not fit on an SM");
+        }
+        g.grid = sms * bps;
+        if ((e = cudaMalloc(&g.d_jobs, sizeof(JobDesc) * nj + sizeof(BatchHead))) != cudaSuccess)
+            return cfail(e, "cudaMalloc(job table)");
+        g.d_head = reinterpret_cast<BatchHead*>(g.d_jobs + nj);
+        if ((e = cudaHostAlloc(&g.h_jobs, sizeof(JobDesc) * nj + sizeof(BatchHead), 0)) != cudaSuccess)
+            return cfail(e, "cudaHostAlloc(job table)");
+        // capture: reset statistics + cursor, persistent kernel
+        BatchArgs ba;
+        ba.jobs = g.d_jobs;
+        ba.njobs = (int)nj;
+        ba.head = g.d_head;
+        cudaGraph_t graph = nullptr;
+        if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cfail(e, "cudaStreamBeginCapture");
+        cudaError_t e1 = launch_batch_reset(g.d_jobs, (int)nj, g.d_head, b->stream);
+        cudaError_t e2 = L.batch(ba, g.color, g.grid, g.smem, b->stream);
+        e = cudaStreamEndCapture(b->stream, &graph);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess)
+        {
+            if (graph)
+                cudaGraphDestroy(graph);
+            return cfail(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e), "graph capture");
+        }
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+            return cfail(e, "cudaGraphInstantiate");
+    }
+    *out = b;
+    return FFR_OK;
+}
+
+void ffr_batch_destroy(ffr_batch* b)
+{
+    batch_free(b);
+}
+
+const char* ffr_batch_last_error(const ffr_batch* b)
+{
+    return b ? b->err.c_str() : g_create_error.c_str();
+}
+
+ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_t* seeds,
+                            uint64_t bad_limit, ffr_stats* stats)
+{
+    if (!b || !samples || !seeds)
+        return FFR_ERR_ARG;
+    BCU(b, cudaSetDevice(b->device));
+    const size_t n = b->ctxs.size();
+    // streams and trajectory length per job, high-word planes where needed
+    for (size_t i = 0; i < n; ++i)
+    {
+        ffr_ctx* c = b->ctxs[i];
+        if (c->count_bound + samples[i] >= 0xFFFFFFFFULL)
+        {
+            ffr_status s = ensure_hi(c);
+            if (s != FFR_OK)
+                return bfail(b, s, c->err);
+        }
+    }
+    for (auto& g : b->groups)
+    {
+        unsigned long long chunk = 0;
+        for (size_t k = 0; k < g.members.size(); ++k)
+        {
+            ffr_ctx* c = b->ctxs[g.members[k]];
+            const uint64_t N = samples[g.members[k]];
+            uint64_t L = c->opts.traj_len ? c->opts.traj_len : b->traj_len;
+            uint64_t S = c->opts.streams ? c->opts.streams
+                                         : std::max<uint64_t>(1, (N + L - 1) / L);
+            if (!c->opts.traj_len && c->opts.streams)
+                L = std::max<uint64_t>(1, (N + S - 1) / S);
+            const uint64_t ntraj = N ? (N + L - 1) / L : 0;
+            const uint64_t active = std::min<uint64_t>(S, ntraj);
+            if ((long double)((ntraj + S - 1) / S) * L >= 4294967296.0L)
+                return bfail(b, FFR_ERR_ARG, "too many samples per GPU thread (raise streams)");
+            JobDesc& jd = g.h_jobs[k];
+            fill_args(c, jd.a, N, seeds[g.members[k]], bad_limit, S, L, c->d_counts, c->d_hi,
+                      c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : 0);
+            jd.chunk_begin = chunk;
+            jd.chunks = (active + 127) / 128;
+            chunk += jd.chunks;
+        }
+        BatchHead* hh = reinterpret_cast<BatchHead*>(g.h_jobs + g.members.size());
+        hh->total_chunks = chunk;
+        hh->cursor = 0;
+        BCU(b, cudaMemcpyAsync(g.d_jobs, g.h_jobs,
+                               sizeof(JobDesc) * g.members.size() + sizeof(BatchHead),
+                               cudaMemcpyHostToDevice, b->stream));
+    }
+    BCU(b, cudaEventRecord(b->ev0, b->stream));
+    for (auto& g : b->groups)
+        BCU(b, cudaGraphLaunch(g.exec, b->stream));
+    BCU(b, cudaEventRecord(b->ev1, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    ffr_status worst = FFR_OK;
+    for (size_t i = 0; i < n; ++i)
+    {
+        ffr_ctx* c = b->ctxs[i];
+        c->count_bound += samples[i];
+        StatsHeadCopy hs;
+        BCU(b, cudaMemcpy(&hs, c->d_stats, sizeof hs, cudaMemcpyDeviceToHost));
+        if (hs.stop)
+            worst = FFR_BAD_VALUES;
+        if (!stats)
+            continue;
+        ffr_stats* st = &stats[i];
+        ffr_status s = read_stats(c, hs, st);
+        if (s != FFR_OK)
+            return bfail(b, s, c->err);
+        st->kernel_ms = ms;
+        st->kernel = FFR_KERNEL_PLAIN;
+    }
+    return worst;
 }
 
 } // extern "C"

@@ -193,7 +193,39 @@ __global__ void atomic_rate_kernel(unsigned int* __restrict__ buf, unsigned int 
     }
 }
 
+// one CTA per job: zero the statistics head and per-xform counts, set the
+// extreme keys to +inf / -inf; CTA 0 also rewinds the claim cursor
+__global__ void batch_reset_kernel(const JobDesc* jobs, int njobs, BatchHead* head)
+{
+    const int j = blockIdx.x;
+    if (j == 0 && threadIdx.x == 0)
+        head->cursor = 0ull;
+    if (j >= njobs)
+        return;
+    DevStats* st = jobs[j].a.stats;
+    const int nxf = jobs[j].a.nxf;
+    if (threadIdx.x == 0)
+    {
+        st->s_iter = st->s_plot = st->bad_total = st->dropped = st->bad_claim = 0ull;
+        st->stop = st->cancelled = 0u;
+        for (int i = 0; i < kMaxDims; ++i)
+        {
+            st->ext_lo[i] = order_key(__longlong_as_double(0x7ff0000000000000ll));
+            st->ext_hi[i] = order_key(__longlong_as_double((long long)0xfff0000000000000ull));
+        }
+    }
+    for (int i = threadIdx.x; i < nxf; i += blockDim.x)
+        st->xf_dist[i] = 0ull;
+}
+
 } // namespace
+
+cudaError_t launch_batch_reset(const JobDesc* jobs, int njobs, BatchHead* head,
+                               cudaStream_t st)
+{
+    batch_reset_kernel<<<njobs > 0 ? njobs : 1, 128, 0, st>>>(jobs, njobs, head);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned int iters,
                                int grid, int block, unsigned int salt, cudaStream_t st)

@@ -67,6 +67,35 @@ cudaError_t FFR_NAME(occupancy)(int color, int spill, int* blocks_per_sm, int* b
                  : occ_one<false>(blocks_per_sm, prog_bytes, nxf, smem);
 }
 
+template <bool C>
+static cudaError_t batch_attr(size_t smem)
+{
+    return cudaFuncSetAttribute(chaos_batch_kernel<FFR_D, Real, C, kBlock>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t FFR_NAME(launch_batch)(const BatchArgs& b, int color, int grid, size_t smem,
+                                   cudaStream_t st)
+{
+    if (color)
+        chaos_batch_kernel<FFR_D, Real, true, kBlock><<<grid, kBlock, smem, st>>>(b);
+    else
+        chaos_batch_kernel<FFR_D, Real, false, kBlock><<<grid, kBlock, smem, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t FFR_NAME(occupancy_batch)(int color, int* blocks_per_sm, int* block, size_t smem)
+{
+    *block = kBlock;
+    cudaError_t e = color ? batch_attr<true>(smem) : batch_attr<false>(smem);
+    if (e != cudaSuccess)
+        return e;
+    return color ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                       blocks_per_sm, chaos_batch_kernel<FFR_D, Real, true, kBlock>, kBlock, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                       blocks_per_sm, chaos_batch_kernel<FFR_D, Real, false, kBlock>, kBlock, smem);
+}
+
 cudaError_t FFR_NAME(launch_step)(const StepArgs& a, cudaStream_t st)
 {
     if (a.npts == 0)

@@ -193,8 +193,12 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
         atomicAdd(&a.counts[bi], 1u);
 }
 
+// Runs streams s_first, s_first + s_stride, ... (below the job's active
+// stream count), then merges this CTA's statistics into a.stats.
 template <int D, typename R, bool COLOR, int BLOCK>
-__device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem)
+__device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem,
+                                           unsigned long long s_first,
+                                           unsigned long long s_stride)
 {
     using T = RealTraits<R>;
     Prog<R> pg;
@@ -236,12 +240,10 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     const unsigned long long L = a.traj_len;
     const unsigned long long ntraj = (a.samples + L - 1) / L;
     const unsigned long long nstreams = a.streams < ntraj ? a.streams : ntraj;
-    const unsigned long long gstride = (unsigned long long)gridDim.x * BLOCK;
     bool stop = false;
     volatile unsigned int* vstop = &a.stats->stop;
 
-    for (unsigned long long s = (unsigned long long)blockIdx.x * BLOCK + threadIdx.x;
-         s < nstreams && !stop; s += gstride)
+    for (unsigned long long s = s_first; s < nstreams && !stop; s += s_stride)
     {
         rng.seed(stream_key(a.seed, s), a.isaac_init);
         for (unsigned long long tj = s; tj < ntraj && !stop; tj += a.streams)
@@ -467,7 +469,66 @@ __global__ void __launch_bounds__(BLOCK, 4) chaos_kernel(const RenderArgs a)
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
     __syncthreads();
-    chaos_body<D, R, COLOR, BLOCK>(a, smem);
+    chaos_body<D, R, COLOR, BLOCK>(a, smem, (unsigned long long)blockIdx.x * BLOCK + threadIdx.x,
+                                   (unsigned long long)gridDim.x * BLOCK);
+}
+
+// Persistent multi-flame render: each CTA claims (job, chunk of BLOCK
+// streams) pairs from a global cursor until the job table is exhausted.  A
+// job's streams are the ones ffr_render would run for that context alone,
+// so every job's buffer is the same alone and in the batch.  The claimed
+// job's arguments are copied to shared memory and its program is reloaded
+// only when the CTA moves to another job.
+template <int D, typename R, bool COLOR, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 4) chaos_batch_kernel(const BatchArgs b)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ __align__(16) RenderArgs s_args;
+    __shared__ unsigned long long s_chunk;
+    __shared__ int s_job;
+    int cur = -1;
+    const unsigned long long total = b.head->total_chunks;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            const unsigned long long c = atomicAdd(&b.head->cursor, 1ull);
+            int j = -1;
+            if (c < total)
+            {
+                int lo = 0, hi = b.njobs - 1;
+                while (lo < hi)
+                {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (b.jobs[mid].chunk_begin <= c)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                j = lo;
+                s_chunk = c - b.jobs[j].chunk_begin;
+            }
+            s_job = j;
+        }
+        __syncthreads();
+        const int j = s_job;
+        if (j < 0)
+            break;
+        if (j != cur)
+        {
+            const unsigned int* src = reinterpret_cast<const unsigned int*>(&b.jobs[j].a);
+            unsigned int* dst = reinterpret_cast<unsigned int*>(&s_args);
+            for (unsigned int k = threadIdx.x; k < sizeof(RenderArgs) / 4; k += BLOCK)
+                dst[k] = src[k];
+            __syncthreads();
+            load_program<BLOCK>(smem, s_args.prog, s_args.prog_bytes);
+            __syncthreads();
+            cur = j;
+        }
+        chaos_body<D, R, COLOR, BLOCK>(s_args, smem, s_chunk * BLOCK + threadIdx.x,
+                                       ~0ull >> 1);
+        __syncthreads();
+    }
 }
 
 // XForm::applyIteration on a batch of points; point k uses stream

@@ -53,6 +53,31 @@ struct RenderArgs
     unsigned long long isaac_init[16];
 };
 
+// One job of a batched launch: the arguments ffr_render would use for the
+// context alone, and its range of chunks (BLOCK streams each) in the
+// batch's chunk order.
+struct JobDesc
+{
+    RenderArgs a;
+    unsigned long long chunk_begin;
+    unsigned long long chunks;
+};
+
+// Device-side header of a batch: chunk count and the claim cursor (reset
+// by batch_reset_kernel before each launch).
+struct BatchHead
+{
+    unsigned long long total_chunks;
+    unsigned long long cursor;
+};
+
+struct BatchArgs
+{
+    const JobDesc* jobs;
+    int njobs;
+    BatchHead* head;
+};
+
 // Single xform application on a batch of points (one stream per point).
 struct StepArgs
 {
@@ -104,6 +129,10 @@ struct IsaacInit
                                              int* blocks_per_sm, int* block,    \
                                              unsigned int prog_bytes, int nxf,  \
                                              int words, size_t* smem);          \
+    cudaError_t launch_batch_p##P##_d##D(const BatchArgs&, int color, int grid, \
+                                         size_t smem, cudaStream_t);            \
+    cudaError_t occupancy_batch_p##P##_d##D(int color, int* blocks_per_sm,      \
+                                            int* block, size_t smem);           \
     cudaError_t launch_step_p##P##_d##D(const StepArgs&, cudaStream_t);         \
     cudaError_t launch_trace_p##P##_d##D(const TraceArgs&, cudaStream_t);
 
@@ -133,6 +162,10 @@ cudaError_t launch_hist_reduce(const unsigned int* counts, const unsigned int* h
 
 cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned int iters,
                                int grid, int block, unsigned int salt, cudaStream_t);
+
+// zero the statistics of every job (one CTA per job) and the batch cursor
+cudaError_t launch_batch_reset(const JobDesc* jobs, int njobs, BatchHead* head,
+                               cudaStream_t);
 
 // monotone u64 key of a double (NaN never stored)
 __host__ __device__ inline unsigned long long order_key(double d)

@@ -39,7 +39,8 @@ EXPORTS = [
     "ffr_info", "ffr_size", "ffr_flame_json", "ffr_add_buffer", "ffr_render",
     "ffr_read_buffer", "ffr_load_buffer", "ffr_histogram", "ffr_clear",
     "ffr_isaac_words", "ffr_step", "ffr_trace", "ffr_plan",
-    "ffr_measure_atomic_rate", "ffr_render_noalloc",
+    "ffr_measure_atomic_rate", "ffr_render_noalloc", "ffr_batch_create",
+    "ffr_batch_destroy", "ffr_batch_render", "ffr_batch_last_error",
 ]
 
 
@@ -113,6 +114,13 @@ def load_library(path: str = LIB_PATH):
         L.ffr_plan.argtypes = [vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
         L.ffr_measure_atomic_rate.argtypes = [ctypes.c_int, u64, u64,
                                               ctypes.POINTER(ctypes.c_double)]
+        L.ffr_batch_create.argtypes = [ctypes.POINTER(vp), sz, ctypes.POINTER(vp)]
+        L.ffr_batch_destroy.argtypes = [vp]
+        L.ffr_batch_destroy.restype = None
+        L.ffr_batch_render.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), u64,
+                                       ctypes.POINTER(Stats)]
+        L.ffr_batch_last_error.argtypes = [vp]
+        L.ffr_batch_last_error.restype = ctypes.c_char_p
         L.ffr_render_noalloc.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts), vp, vp,
                                          u64, u64, u64, u64, ctypes.POINTER(Stats)]
         for name in EXPORTS:
@@ -308,3 +316,60 @@ def create_status(flame_text: str, precision: int = FP64):
     if st == FFR_OK:
         lib.ffr_destroy(ctx)
     return st, msg
+
+
+class Batch:
+    """Several BufferRenderers rendered in one persistent launch per
+    (dims, colour) group (ffr_batch_*); each buffer equals a solo render."""
+
+    def __init__(self, renderers):
+        self._lib = load_library()
+        self.renderers = list(renderers)
+        arr = (ctypes.c_void_p * len(self.renderers))(*[r._ctx.value for r in self.renderers])
+        out = ctypes.c_void_p()
+        st = self._lib.ffr_batch_create(arr, len(self.renderers), ctypes.byref(out))
+        if st != FFR_OK:
+            raise FfrError(st, self._lib.ffr_last_error(None).decode("utf-8", "replace"))
+        self._b = out
+
+    def render(self, samples, seeds, bad_limit: int = 256, stats: bool = True):
+        n = len(self.renderers)
+        sa = (ctypes.c_uint64 * n)(*samples)
+        se = (ctypes.c_uint64 * n)(*seeds)
+        sts = (Stats * n)() if stats else None
+        status = self._lib.ffr_batch_render(self._b, sa, se, bad_limit, sts)
+        if status not in (FFR_OK, FFR_BAD_VALUES):
+            raise FfrError(status, self._lib.ffr_batch_last_error(self._b).decode("utf-8", "replace"))
+        if not stats:
+            return status, None
+        out = []
+        for i, r in enumerate(self.renderers):
+            st = sts[i]
+            d = r.dims
+            out.append(RenderStats(
+                status=status, samples_iterated=st.samples_iterated,
+                samples_plotted=st.samples_plotted, bad_values=st.bad_values,
+                dropped=st.dropped, ext_lo=np.array(st.ext_lo[:d]),
+                ext_hi=np.array(st.ext_hi[:d]),
+                xf_dist=np.array(st.xf_dist[:min(int(st.xform_ids), MAX_XFORM_IDS)], dtype=np.uint64),
+                bad_xf=np.array(st.bad_xf[:st.bad_recorded], dtype=np.uint64),
+                bad_pts=np.zeros((0, d)), streams=st.streams, traj_len=st.traj_len,
+                settle=st.settle, kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg))
+        return status, out
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._lib.ffr_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

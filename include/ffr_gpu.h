@@ -164,6 +164,33 @@ ffr_status ffr_histogram(ffr_ctx *ctx, uint64_t *sum, uint64_t *min,
 ffr_status ffr_clear(ffr_ctx *ctx);
 
 /* ---------------------------------------------------------------------
+ * Batched render: many flames (contexts on one device, one precision) in
+ * one persistent launch per (dims, colour) group, replayed from a captured
+ * CUDA graph.  No single reference counterpart: it runs, for every context,
+ * exactly what ffr_render would run for it alone (same streams, same
+ * trajectories), so each buffer is identical to a solo render of the same
+ * samples and seed.  Work is split into chunks of one CTA's worth of
+ * streams claimed from a global cursor, so flames of very different sizes
+ * and sample counts share the GPU without stragglers.
+ * ------------------------------------------------------------------- */
+typedef struct ffr_batch ffr_batch;
+
+/* Group n contexts (not owned; they must outlive the batch). */
+ffr_status ffr_batch_create(ffr_ctx *const *ctxs, size_t n, ffr_batch **out);
+void ffr_batch_destroy(ffr_batch *b);
+
+/* Render samples[i] samples with seeds[i] into context i, for all i at
+   once.  stats may be NULL or an array of n (each filled as ffr_render
+   would); returns the first non-OK status (FFR_BAD_VALUES if any job hit
+   its bad-value limit). */
+ffr_status ffr_batch_render(ffr_batch *b, const uint64_t *samples,
+                            const uint64_t *seeds, uint64_t bad_limit,
+                            ffr_stats *stats);
+
+/* Message of the last failing call on b. */
+const char *ffr_batch_last_error(const ffr_batch *b);
+
+/* ---------------------------------------------------------------------
  * Verification entry points: the same device code as ffr_render, exposed
  * one function at a time so each can be checked against the reference.
  * ------------------------------------------------------------------- */
