@@ -22,7 +22,23 @@ roofline  binned samples x 8 B (one 4-byte atomic read-modify-write each)
 cpu_baseline  the oracle's C restatement of the reference path (FP64,
         all host threads) on a bounded sample of the same workload
 
+tv      FP32 against FP64 at a fixed sample count: total-variation distance
+        between the FP32 histogram and an FP64 (reference arithmetic) one,
+        beside the FP64 seed-to-seed noise floor at the same count
+
 --impl reference times that CPU implementation alone, as the reference arm.
+
+Other configurations (--workload; each prints its own JSON line):
+  sierpinski  2-D Sierpinski triangle, 1024x1024, 1e8 samples from 1e6
+              trajectories of 100, settle 20, seed 1, FP64 (the plain method)
+              and FP32; --verify compares the FP64 buffer with the oracle
+  tetra3d     Sierpinski tetrahedron, 512^3 u32 buffer (512 MiB), 1e10
+              samples in steps of 1e9, FP32, seed 3
+  batch256    256 random 2-D flames (2..8 xforms, square buffers of side
+              256..2048, 1e7..1e9 samples each, seed 11) in one persistent
+              graph-captured launch per step, FP32
+  serving     Poisson request stream (200 req/s for 60 s, seed 23) through
+              the serving loop: p50/p99 latency and samples/s
 """
 from __future__ import annotations
 
@@ -185,20 +201,359 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tv_distance(a, b) -> float:
+    """1/2 sum |a/sum a - b/sum b| over all cells."""
+    import numpy as np
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return 0.5 * float(np.abs(a / a.sum() - b / b.sum()).sum())
+
+
+def tv_check(ffr, text, n, settle, device, seeds=(101, 202, 303)):
+    """TV of an FP32 histogram against an FP64 one at n samples, and the FP64
+    seed-to-seed noise floor at the same n."""
+    hs = []
+    for prec, seed in ((ffr.FP64, seeds[0]), (ffr.FP64, seeds[1]), (ffr.FP32, seeds[2])):
+        with ffr.BufferRenderer(text, precision=prec, settle=settle, device=device) as r:
+            r.render(n, seed, bad_limit=10**12)
+            hs.append(r.counts())
+    floor = tv_distance(hs[0], hs[1])
+    d = tv_distance(hs[2], hs[0])
+    return {"samples": n, "fp32_vs_fp64": d, "fp64_noise_floor": floor,
+            "ratio": d / floor if floor > 0 else None, "bar": 3.0}
+
+
+def _flames():
+    return ge._load("ffr_flames", os.path.join(ROOT, "flame-fractal-renderer_gb300", "flames.py"))
+
+
+def _setup_single(args):
+    """Single-GPU workloads: rank 0 only (the other ranks exit)."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return None
+    import torch
+    torch.cuda.set_device(local)
+    ge.build()
+    return ge.package(), local
+
+
+def _line(args, workload, value, ms_per_step, dtype, config, **extra):
+    peaks, _ = measured_peaks()
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": "synthetic (seeded flame generator)",
+            "config": dict({"workload": workload}, **config)}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def _timed_steps(r, args, samples, seed0, flush=None):
+    """args.warmup untimed renders, then args.steps timed ones; returns
+    (kernel ms, binned, iterated, last stats)."""
+    import torch
+    for w in range(args.warmup):
+        r.render(samples, seed0 + 10_000 + w, bad_limit=10**12)
+    r.clear()
+    ms = 0.0
+    binned = iters = 0
+    s = None
+    for k in range(args.steps):
+        if flush is not None:
+            flush.zero_()
+            torch.cuda.synchronize()
+        s = r.render(samples, seed0 + k, bad_limit=10**12)
+        ms += s.kernel_ms
+        binned += s.samples_plotted - s.dropped
+        iters += s.samples_iterated
+    return ms, binned, iters, s
+
+
+def run_sierpinski(args):
+    """2-D Sierpinski triangle, 1024^2, 1e8 samples from 1e6 trajectories of
+    100 samples, settle 20, seed 1: the plain FP64 method and FP32."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    import torch
+    text = json.dumps(_flames().sierpinski_2d((1024, 1024)))
+    N, T, Lt, settle = 10**8, 10**6, 100, 20
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    res = {}
+    sampler = ClockSampler(dev)
+    sampler.start()
+    for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
+        with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
+                                device=dev) as r:
+            ms, binned, iters, s = _timed_steps(r, args, N, 1, flush)
+            res[name] = {"value": binned / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                         "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel)}
+            if name == "fp64" and args.verify:
+                r.clear()
+                r.render(N, 1, bad_limit=10**12)
+                gpu = r.counts()
+    clocks = sampler.stop()
+    verify = None
+    if args.verify:
+        fo = ge._load("flame_oracle", os.path.join(ROOT, "oracle", "flame_oracle.py"))
+        fo.build()
+        of = fo.OracleFlame(fo.load_flame(text))
+        ref = fo.render(of, 1, T, N, Lt, settle, 10**12, os.cpu_count() or 1)
+        import numpy as np
+        verify = {"identical_to_oracle": bool(np.array_equal(gpu, ref.counts)),
+                  "binned": int(gpu.sum())}
+    atom = ffr.measure_atomic_rate(1024 * 1024, 1 << 31, device=dev)
+    v = res["fp64"]["value"]
+    _line(args, "2-D Sierpinski triangle, 1024x1024, 1e8 samples from 1e6 trajectories",
+          v, res["fp64"]["ms_per_step"], "f64",
+          {"samples_per_step": N, "trajectories": T, "traj_len": Lt, "settle": settle,
+           "seed": 1, "flush": "256 MiB L2 flush between timed steps"},
+          fp32=res["fp32"], gpu_launches=args.steps * 2,
+          l2_atomic={"peak_ops_per_s": atom, "frac_fp64": v / atom,
+                     "frac_fp32": res["fp32"]["value"] / atom},
+          verify=verify, clocks=clocks)
+
+
+def run_tetra3d(args):
+    """Sierpinski tetrahedron, 512^3 u32 buffer, 1e10 samples in steps of
+    1e9, FP32, seed 3."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    text = json.dumps(_flames().tetrahedron_3d((512, 512, 512)))
+    B, settle = int(args.samples_per_step), 20
+    with ffr.BufferRenderer(text, precision=ffr.FP32, settle=settle, device=dev) as r:
+        sampler = ClockSampler(dev)
+        sampler.start()
+        # the 512 MiB buffer exceeds L2: no flush needed between steps
+        ms, binned, iters, s = _timed_steps(r, args, B, 3)
+        clocks = sampler.stop()
+        assert r.histogram()[0] == binned
+    value = binned / (ms * 1e-3)
+    peaks, kind = measured_peaks()
+    achieved = 8.0 * binned / (ms * 1e-3) / 1e9
+    atom = ffr.measure_atomic_rate(512 ** 3, 1 << 31, device=dev)
+    tv = None if args.no_tv else tv_check(ffr, text, 10**8, settle, dev)
+    _line(args, "Sierpinski tetrahedron, 512^3 u32 buffer, 1e10 samples", value,
+          ms / args.steps, "f32",
+          {"samples_per_step": B, "settle": settle, "seed": 3, "streams": s.streams,
+           "traj_len": s.traj_len, "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel),
+           "flush": "none: the 512 MiB buffer is larger than L2"},
+          gpu_launches=args.steps,
+          roofline={"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                    "peak_source": kind},
+          l2_atomic={"peak_ops_per_s": atom, "achieved_ops_per_s": value, "frac": value / atom,
+                     "what": "u32 atomic adds at uniformly random cells of a 512^3 buffer"},
+          tv=tv, clocks=clocks, iterated_per_s=iters / (ms * 1e-3))
+
+
+def run_batch256(args):
+    """256 random 2-D flames in one persistent, graph-captured launch per step."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    import torch
+    fl = _flames()
+    jobs = fl.batch_jobs(11)
+    texts = [json.dumps(f) for f, _ in jobs]
+    ns = [n for _, n in jobs]
+    rs = [ffr.BufferRenderer(t, precision=ffr.FP32, settle=20, traj_len=4096, device=dev)
+          for t in texts]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    with ffr.Batch(rs) as b:
+        for w in range(args.warmup):
+            b.render([max(1, n // 100) for n in ns], [500 + i for i in range(len(ns))],
+                     bad_limit=10**12, stats=False)
+        for r in rs:
+            r.clear()
+        sampler = ClockSampler(dev)
+        sampler.start()
+        ms, binned = 0.0, 0
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            _, sts = b.render(ns, [1000 * k + i for i in range(len(ns))], bad_limit=10**12)
+            ms += sts[0].kernel_ms
+            binned += sum(st.samples_plotted - st.dropped for st in sts)
+        clocks = sampler.stop()
+    for r in rs:
+        r.close()
+    value = binned / (ms * 1e-3)
+    tvs = []
+    if not args.no_tv:
+        for i in range(0, len(texts), len(texts) // 8):
+            t = tv_check(ffr, texts[i], 10**8, 20, dev)
+            t["flame"] = i
+            tvs.append(t)
+    _line(args, "256 random 2-D flames (2-8 xforms, 256^2-2048^2, 1e7-1e9 samples) "
+          "in one persistent launch", value, ms / args.steps, "f32",
+          {"flames": len(texts), "samples_per_step": sum(ns), "settle": 20, "seed": 11,
+           "traj_len": 4096, "kernel": "persistent batch (CUDA graph)",
+           "flush": "256 MiB L2 flush between timed steps"},
+          gpu_launches=args.steps * 2,
+          tv={"per_flame": tvs,
+              "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
+          clocks=clocks)
+
+
+def run_serving(args):
+    """Poisson request stream through the serving loop (ffr_server_*)."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    import queue
+    import random
+    import numpy as np
+    fl = _flames()
+    reqs = fl.serving_requests(23, args.rate, args.duration)
+    texts = [json.dumps(f) if f is not None else None for _, _, f, _ in reqs]
+    geo = []
+    for _, kind, f, _ in reqs:
+        if f is None:
+            geo.append(None)
+        else:
+            cells = 1
+            for x in f["size"]:
+                cells *= x
+            geo.append((cells, f["dimensions"]))
+    srv = ffr.Server(precision=ffr.FP32, settle=20, traj_len=4096, device=dev,
+                     max_active=args.max_active)
+    # warm-up: a few small jobs of each kind (module load, pool growth)
+    for w in range(max(1, args.warmup)):
+        a = srv.submit(texts[0], 10**6, 9000 + w)
+        srv.wait(a, 60_000)
+        srv.release(a)
+    lock = threading.Lock()
+    done = queue.Queue()
+    pool = []                    # resident continuation targets
+    evicted = set()
+    info = {}                    # job -> (kind, cells, dims)
+    rnd = random.Random(23)
+    t_start = time.perf_counter()
+    errors = []
+
+    def submitter():
+        for i, (t, kind, f, n) in enumerate(reqs):
+            dt = t_start + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            try:
+                if kind == "cont":
+                    with lock:
+                        if not pool:
+                            continue
+                        parent = rnd.choice(pool)
+                        j = srv.continue_(parent, n, 50_000 + i)
+                        info[j] = ("cont",) + info[parent][1:]
+                else:
+                    j = srv.submit(texts[i], n, 50_000 + i)
+                    with lock:
+                        info[j] = (kind,) + geo[i]
+                        pool.append(j)
+                        if len(pool) > 64:
+                            evicted.add(pool.pop(0))
+                done.put(j)
+            except Exception as e:          # noqa: BLE001
+                errors.append(repr(e))
+        for _ in range(4):
+            done.put(None)
+
+    results = []
+
+    def completer():
+        while True:
+            j = done.get()
+            if j is None:
+                return
+            try:
+                inf = srv.wait(j, 0)
+                kind, cells, dims = info[j]
+                st = srv.stats(j, dims)
+                t0 = time.perf_counter_ns()
+                out = np.empty(cells, dtype=np.uint64)
+                srv.read_into(j, out.ctypes.data, out.nbytes)
+                t_read = time.perf_counter_ns() - t0
+            except Exception as e:          # noqa: BLE001
+                errors.append(repr(e))
+                continue
+            with lock:
+                keep = j in pool
+                results.append((kind, inf.submit_ns, inf.done_ns, t_read, st.samples_plotted,
+                                st.samples_iterated, inf.status))
+            if not keep:
+                srv.release(j)
+                with lock:
+                    evicted.discard(j)
+
+    sampler = ClockSampler(dev)
+    sampler.start()
+    th = [threading.Thread(target=submitter)] + [threading.Thread(target=completer)
+                                                  for _ in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t_start
+    clocks = sampler.stop()
+    load = srv.load()
+    srv.close()
+    lat = np.array([(d - s) * 1e-6 for _, s, d, _, _, _, _ in results])
+    lat_read = np.array([(d - s) * 1e-6 + r * 1e-6 for _, s, d, r, _, _, _ in results])
+    binned = sum(r[4] for r in results)
+    iters = sum(r[5] for r in results)
+    first = min(r[1] for r in results)
+    last = max(r[2] for r in results)
+    span = (last - first) * 1e-9
+    offered = sum(n for *_, n in reqs) / args.duration
+    kinds = {}
+    for r in results:
+        kinds.setdefault(r[0], []).append((r[2] - r[1]) * 1e-6)
+    _line(args, f"Poisson serving stream, {args.rate:g} req/s for {args.duration:g} s "
+          "(80% 2-D, 15% 3-D, 5% continuations)", binned / span, span * 1e3, "f32",
+          {"requests": len(reqs), "completed": len(results), "rate_per_s": args.rate,
+           "duration_s": args.duration, "seed": 23, "settle": 20, "traj_len": 4096,
+           "max_active": args.max_active, "flush": "n/a (a stream of distinct buffers)"},
+          latency_ms={"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "p50_with_read": float(np.percentile(lat_read, 50)),
+                      "p99_with_read": float(np.percentile(lat_read, 99)),
+                      "by_kind_p50": {k: float(np.percentile(v, 50)) for k, v in kinds.items()},
+                      "by_kind_p99": {k: float(np.percentile(v, 99)) for k, v in kinds.items()}},
+          offered_samples_per_s=offered, iterated_per_s=iters / span, wall_s=wall,
+          statuses=sorted({r[6] for r in results}), errors=errors[:5],
+          server_load=load, clocks=clocks)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="random2d",
+                    choices=["random2d", "sierpinski", "tetra3d", "batch256", "serving"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--samples-per-step", type=float, default=1e9)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-tv", action="store_true")
+    ap.add_argument("--verify", action="store_true")
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--max-active", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "random2d":
+        {"sierpinski": run_sierpinski, "tetra3d": run_tetra3d, "batch256": run_batch256,
+         "serving": run_serving}[args.workload](args)
         return
     ws, rank, local = dist_env()
     import torch
@@ -323,6 +678,10 @@ def main():
                 "kernel": "plain FP64 mirror",
                 "fp32_over_fp64": value / ws / (bin64 / (ms64 * 1e-3))}
 
+    tv = None
+    if not args.no_tv:
+        tv = tv_check(ffr, text, 2 * 10**8, settle, local)
+
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
@@ -348,6 +707,7 @@ def main():
         "roofline": roofline,
         "l2_atomic": l2,
         "fp64": fp64,
+        "tv": tv,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "iterated_per_s": iters / (kern_ms * 1e-3),

@@ -81,7 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
-    for name in ("api", "flame", "json", "variations_host"):
+    for name in ("api", "server", "flame", "json", "variations_host"):
         src = os.path.join(CSRC, name + ".cpp")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [*cxx_common, "-c", src, "-o", obj]))

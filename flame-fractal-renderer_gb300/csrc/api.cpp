@@ -67,26 +67,6 @@ void ffr::set_global_error(const std::string& m)
 
 namespace {
 
-typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
-typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
-typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
-typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
-typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
-typedef cudaError_t (*BatchFn)(const BatchArgs&, int, int, size_t, cudaStream_t);
-typedef cudaError_t (*OccBatchFn)(int, int*, int*, size_t);
-
-struct Launchers
-{
-    RenderFn render;
-    OccFn occ;
-    RenderFn sorted;
-    OccSortedFn occ_sorted;
-    BatchFn batch;
-    OccBatchFn occ_batch;
-    StepFn step;
-    TraceFn trace;
-};
-
 const Launchers kLaunchers[2][3] = {
     {
         {launch_render_p0_d1, occupancy_p0_d1, launch_sorted_p0_d1,
@@ -113,6 +93,11 @@ const Launchers kLaunchers[2][3] = {
 };
 
 } // namespace
+
+const Launchers& ffr::launchers(int precision, int dims)
+{
+    return kLaunchers[precision][dims - 1];
+}
 
 struct ffr_ctx
 {
@@ -1270,6 +1255,7 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
                       c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : 0);
             jd.chunk_begin = chunk;
             jd.chunks = (active + 127) / 128;
+            jd.chunk_first = 0;
             chunk += jd.chunks;
         }
         BatchHead* hh = reinterpret_cast<BatchHead*>(g.h_jobs + g.members.size());

@@ -193,17 +193,10 @@ __global__ void atomic_rate_kernel(unsigned int* __restrict__ buf, unsigned int 
     }
 }
 
-// one CTA per job: zero the statistics head and per-xform counts, set the
-// extreme keys to +inf / -inf; CTA 0 also rewinds the claim cursor
-__global__ void batch_reset_kernel(const JobDesc* jobs, int njobs, BatchHead* head)
+// zero one statistics head and its per-xform counts, extreme keys to
+// +inf / -inf (one CTA)
+__device__ void reset_one(DevStats* st, int nxf)
 {
-    const int j = blockIdx.x;
-    if (j == 0 && threadIdx.x == 0)
-        head->cursor = 0ull;
-    if (j >= njobs)
-        return;
-    DevStats* st = jobs[j].a.stats;
-    const int nxf = jobs[j].a.nxf;
     if (threadIdx.x == 0)
     {
         st->s_iter = st->s_plot = st->bad_total = st->dropped = st->bad_claim = 0ull;
@@ -218,12 +211,34 @@ __global__ void batch_reset_kernel(const JobDesc* jobs, int njobs, BatchHead* he
         st->xf_dist[i] = 0ull;
 }
 
+// one CTA per job: reset its statistics; CTA 0 also rewinds the claim cursor
+__global__ void batch_reset_kernel(const JobDesc* jobs, int njobs, BatchHead* head)
+{
+    const int j = blockIdx.x;
+    if (j == 0 && threadIdx.x == 0)
+        head->cursor = 0ull;
+    if (j >= njobs)
+        return;
+    reset_one(jobs[j].a.stats, jobs[j].a.nxf);
+}
+
+__global__ void stats_reset_kernel(DevStats* st, int nxf)
+{
+    reset_one(st, nxf);
+}
+
 } // namespace
 
 cudaError_t launch_batch_reset(const JobDesc* jobs, int njobs, BatchHead* head,
                                cudaStream_t st)
 {
     batch_reset_kernel<<<njobs > 0 ? njobs : 1, 128, 0, st>>>(jobs, njobs, head);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stats_reset(DevStats* st, int nxf, cudaStream_t s)
+{
+    stats_reset_kernel<<<1, 128, 0, s>>>(st, nxf);
     return cudaGetLastError();
 }
 

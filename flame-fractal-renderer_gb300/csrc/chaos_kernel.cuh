@@ -26,22 +26,7 @@
 
 namespace ffr {
 
-constexpr int kLocalXfCounters = 16;
 constexpr int kStopPollMask = 4095;     // poll stop/cancel every 4096 samples
-
-__host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
-
-template <int BLOCK>
-__host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf)
-{
-    size_t s = align16u(prog_bytes);
-    s += 2 * 16 * (size_t)BLOCK * sizeof(uint64_t);
-    if (nxf <= kLocalXfCounters)
-        s += (size_t)nxf * BLOCK * sizeof(uint32_t);
-    else
-        s += (size_t)nxf * sizeof(unsigned long long);
-    return s;
-}
 
 // Program view over the shared-memory copy
 template <typename R>
@@ -506,7 +491,7 @@ __global__ void __launch_bounds__(BLOCK, 4) chaos_batch_kernel(const BatchArgs b
                         hi = mid - 1;
                 }
                 j = lo;
-                s_chunk = c - b.jobs[j].chunk_begin;
+                s_chunk = c - b.jobs[j].chunk_begin + b.jobs[j].chunk_first;
             }
             s_job = j;
         }

@@ -53,14 +53,36 @@ struct RenderArgs
     unsigned long long isaac_init[16];
 };
 
+constexpr int kLocalXfCounters = 16;
+
+__host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
+
+// Dynamic shared memory of the plain and batch render kernels: the program,
+// ISAAC state [16][BLOCK] x2, and per-thread u32 xform counters when
+// nxf <= kLocalXfCounters, else one u64 counter per xform for the CTA.
+template <int BLOCK>
+__host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf)
+{
+    size_t s = align16u(prog_bytes);
+    s += 2 * 16 * (size_t)BLOCK * sizeof(uint64_t);
+    if (nxf <= kLocalXfCounters)
+        s += (size_t)nxf * BLOCK * sizeof(uint32_t);
+    else
+        s += (size_t)nxf * sizeof(unsigned long long);
+    return s;
+}
+
 // One job of a batched launch: the arguments ffr_render would use for the
 // context alone, and its range of chunks (BLOCK streams each) in the
-// batch's chunk order.
+// batch's chunk order.  The launch runs the job's chunks chunk_first ..
+// chunk_first + chunks - 1 (chunk k = streams k*BLOCK .. k*BLOCK+BLOCK-1), so
+// a job can be split over several launches (the serving loop's rounds).
 struct JobDesc
 {
     RenderArgs a;
     unsigned long long chunk_begin;
     unsigned long long chunks;
+    unsigned long long chunk_first;
 };
 
 // Device-side header of a batch: chunk count and the claim cursor (reset
@@ -143,6 +165,30 @@ FFR_DECLARE_LAUNCHERS(1, 1)
 FFR_DECLARE_LAUNCHERS(1, 2)
 FFR_DECLARE_LAUNCHERS(1, 3)
 
+typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
+typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
+typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
+typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
+typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
+typedef cudaError_t (*BatchFn)(const BatchArgs&, int, int, size_t, cudaStream_t);
+typedef cudaError_t (*OccBatchFn)(int, int*, int*, size_t);
+
+// the launch functions of one (precision, dims) kernel instantiation
+struct Launchers
+{
+    RenderFn render;
+    OccFn occ;
+    RenderFn sorted;
+    OccSortedFn occ_sorted;
+    BatchFn batch;
+    OccBatchFn occ_batch;
+    StepFn step;
+    TraceFn trace;
+};
+
+// precision 0 (FP64) or 1 (FP32), dims 1..3 (api.cpp)
+const Launchers& launchers(int precision, int dims);
+
 // buffer_kernels.cu
 cudaError_t launch_isaac_words(unsigned long long key, unsigned long long n,
                                unsigned long long* out,
@@ -166,6 +212,9 @@ cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned i
 // zero the statistics of every job (one CTA per job) and the batch cursor
 cudaError_t launch_batch_reset(const JobDesc* jobs, int njobs, BatchHead* head,
                                cudaStream_t);
+
+// zero one statistics block (nxf per-xform counters), extremes to +/-inf
+cudaError_t launch_stats_reset(DevStats* st, int nxf, cudaStream_t);
 
 // monotone u64 key of a double (NaN never stored)
 __host__ __device__ inline unsigned long long order_key(double d)

@@ -41,7 +41,13 @@ EXPORTS = [
     "ffr_isaac_words", "ffr_step", "ffr_trace", "ffr_plan",
     "ffr_measure_atomic_rate", "ffr_render_noalloc", "ffr_batch_create",
     "ffr_batch_destroy", "ffr_batch_render", "ffr_batch_last_error",
+    "ffr_server_default_opts", "ffr_server_create", "ffr_server_destroy",
+    "ffr_server_last_error", "ffr_server_submit", "ffr_server_continue",
+    "ffr_server_poll", "ffr_server_wait", "ffr_server_job_stats", "ffr_server_read",
+    "ffr_server_cancel", "ffr_server_release", "ffr_server_load",
 ]
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
 
 
 class FfrError(RuntimeError):
@@ -72,6 +78,21 @@ class Stats(ctypes.Structure):
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
                 ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32)]
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_uint32), ("device", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("settle", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
+                ("hbm_budget", ctypes.c_uint64), ("max_active", ctypes.c_uint64),
+                ("round_chunks", ctypes.c_uint64), ("timeout_ms", ctypes.c_uint64)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("samples", ctypes.c_uint64), ("buffer_bytes", ctypes.c_uint64),
+                ("parent", ctypes.c_uint64), ("submit_ns", ctypes.c_uint64),
+                ("admit_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64)]
 
 
 _lib = None
@@ -123,6 +144,23 @@ def load_library(path: str = LIB_PATH):
         L.ffr_batch_last_error.restype = ctypes.c_char_p
         L.ffr_render_noalloc.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts), vp, vp,
                                          u64, u64, u64, u64, ctypes.POINTER(Stats)]
+        P = ctypes.POINTER
+        L.ffr_server_default_opts.argtypes = [P(ServerOpts)]
+        L.ffr_server_default_opts.restype = None
+        L.ffr_server_create.argtypes = [P(ServerOpts), P(vp)]
+        L.ffr_server_destroy.argtypes = [vp]
+        L.ffr_server_destroy.restype = None
+        L.ffr_server_last_error.argtypes = [vp]
+        L.ffr_server_last_error.restype = ctypes.c_char_p
+        L.ffr_server_submit.argtypes = [vp, ctypes.c_char_p, sz, vp, sz, u64, u64, u64, P(u64)]
+        L.ffr_server_continue.argtypes = [vp, u64, u64, u64, u64, P(u64)]
+        L.ffr_server_poll.argtypes = [vp, u64, P(JobInfo)]
+        L.ffr_server_wait.argtypes = [vp, u64, u64, P(JobInfo)]
+        L.ffr_server_job_stats.argtypes = [vp, u64, P(Stats)]
+        L.ffr_server_read.argtypes = [vp, u64, vp, sz]
+        L.ffr_server_cancel.argtypes = [vp, u64]
+        L.ffr_server_release.argtypes = [vp, u64]
+        L.ffr_server_load.argtypes = [vp, P(u64), P(u64), P(u64), P(u64)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is ctypes.c_int:      # default: ffr_status
@@ -164,6 +202,20 @@ class RenderStats:
     @property
     def ok(self) -> bool:
         return self.status == FFR_OK
+
+
+def _render_stats(status: int, st: Stats, n: int) -> RenderStats:
+    nrec = st.bad_recorded
+    ids = int(st.xform_ids)
+    return RenderStats(
+        status=status, samples_iterated=st.samples_iterated,
+        samples_plotted=st.samples_plotted, bad_values=st.bad_values,
+        dropped=st.dropped, ext_lo=np.array(st.ext_lo[:n]), ext_hi=np.array(st.ext_hi[:n]),
+        xf_dist=np.array(st.xf_dist[:min(ids, MAX_XFORM_IDS)], dtype=np.uint64),
+        bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
+        bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
+        streams=st.streams, traj_len=st.traj_len, settle=st.settle,
+        kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg)
 
 
 def isaac_words(key: int, n: int, device: int = 0) -> np.ndarray:
@@ -246,18 +298,7 @@ class BufferRenderer:
         status = _check(self._lib, self._ctx,
                         self._lib.ffr_render(self._ctx, samples, seed, bad_limit,
                                              ctypes.byref(st)))
-        n = self.dims
-        nrec = st.bad_recorded
-        ids = int(st.xform_ids)
-        return RenderStats(
-            status=status, samples_iterated=st.samples_iterated,
-            samples_plotted=st.samples_plotted, bad_values=st.bad_values,
-            dropped=st.dropped, ext_lo=np.array(st.ext_lo[:n]), ext_hi=np.array(st.ext_hi[:n]),
-            xf_dist=np.array(st.xf_dist[:min(ids, MAX_XFORM_IDS)], dtype=np.uint64),
-            bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
-            bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
-            streams=st.streams, traj_len=st.traj_len, settle=st.settle,
-            kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg)
+        return _render_stats(status, st, self.dims)
 
     def plan(self, samples: int):
         s, L = ctypes.c_uint64(), ctypes.c_uint64()
@@ -361,6 +402,132 @@ class Batch:
         if getattr(self, "_b", None):
             self._lib.ffr_batch_destroy(self._b)
             self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+@dataclass
+class Job:
+    id: int
+    state: int
+    status: int
+    samples: int
+    buffer_bytes: int
+    parent: int
+    submit_ns: int
+    admit_ns: int
+    done_ns: int
+
+    @property
+    def finished(self) -> bool:
+        return self.state in (JOB_DONE, JOB_FAILED, JOB_CANCELLED)
+
+    @property
+    def latency_s(self) -> float:
+        return (self.done_ns - self.submit_ns) * 1e-9
+
+
+class Server:
+    """Serving loop (ffr_server_*): jobs submitted at any time run in
+    continuously batched rounds with their buffers resident on the device."""
+
+    def __init__(self, precision: int = FP32, settle: int = 53, traj_len: int = 4096,
+                 device: int = 0, hbm_budget: int = 0, max_active: int = 256,
+                 round_chunks: int = 0, timeout_ms: int = 0):
+        self._lib = load_library()
+        o = ServerOpts()
+        self._lib.ffr_server_default_opts(ctypes.byref(o))
+        o.device, o.precision, o.settle, o.traj_len = device, precision, settle, traj_len
+        o.hbm_budget, o.max_active, o.round_chunks = hbm_budget, max_active, round_chunks
+        o.timeout_ms = timeout_ms
+        out = ctypes.c_void_p()
+        st = self._lib.ffr_server_create(ctypes.byref(o), ctypes.byref(out))
+        if st != FFR_OK:
+            raise FfrError(st, self._lib.ffr_last_error(None).decode("utf-8", "replace"))
+        self._s = out
+        self.settle, self.traj_len = settle, traj_len
+
+    def _check(self, status: int):
+        if status not in (FFR_OK, FFR_BAD_VALUES):
+            raise FfrError(status, self._lib.ffr_server_last_error(self._s).decode("utf-8", "replace"))
+        return status
+
+    def submit(self, flame, samples: int, seed: int, bad_limit: int = 256, init=None) -> int:
+        text = flame if isinstance(flame, str) else json.dumps(flame)
+        raw = text.encode("utf-8")
+        job = ctypes.c_uint64()
+        if init is None:
+            ip, n = None, 0
+        else:
+            buf = np.frombuffer(init, dtype=np.uint8) if isinstance(init, (bytes, bytearray)) \
+                else np.ascontiguousarray(init).view(np.uint8)
+            ip, n = _ptr(buf), buf.nbytes
+        self._check(self._lib.ffr_server_submit(self._s, raw, len(raw), ip, n, samples, seed,
+                                                bad_limit, ctypes.byref(job)))
+        return job.value
+
+    def continue_(self, parent: int, samples: int, seed: int, bad_limit: int = 256) -> int:
+        job = ctypes.c_uint64()
+        self._check(self._lib.ffr_server_continue(self._s, parent, samples, seed, bad_limit,
+                                                  ctypes.byref(job)))
+        return job.value
+
+    @staticmethod
+    def _job(job: int, i: JobInfo) -> Job:
+        return Job(job, i.state, i.status, i.samples, i.buffer_bytes, i.parent, i.submit_ns,
+                   i.admit_ns, i.done_ns)
+
+    def poll(self, job: int) -> Job:
+        i = JobInfo()
+        self._check(self._lib.ffr_server_poll(self._s, job, ctypes.byref(i)))
+        return self._job(job, i)
+
+    def wait(self, job: int, timeout_ms: int = 0) -> Job:
+        i = JobInfo()
+        self._check(self._lib.ffr_server_wait(self._s, job, timeout_ms, ctypes.byref(i)))
+        return self._job(job, i)
+
+    def stats(self, job: int, dims: int) -> RenderStats:
+        st = Stats()
+        status = self._check(self._lib.ffr_server_job_stats(self._s, job, ctypes.byref(st)))
+        return _render_stats(status, st, dims)
+
+    def read(self, job: int, cells: int, color_dims: int = 0) -> np.ndarray:
+        """The job's buffer in the file layout, uint64 [cells, 1 + color_dims]."""
+        out = np.zeros((cells, 1 + color_dims), dtype=np.uint64)
+        self._check(self._lib.ffr_server_read(self._s, job, _ptr(out), out.nbytes))
+        return out
+
+    def read_into(self, job: int, ptr: int, nbytes: int) -> None:
+        self._check(self._lib.ffr_server_read(self._s, job, ctypes.c_void_p(ptr), nbytes))
+
+    def cancel(self, job: int) -> None:
+        self._check(self._lib.ffr_server_cancel(self._s, job))
+
+    def release(self, job: int) -> None:
+        self._check(self._lib.ffr_server_release(self._s, job))
+
+    def load(self):
+        q, r, u, p = (ctypes.c_uint64() for _ in range(4))
+        self._check(self._lib.ffr_server_load(self._s, ctypes.byref(q), ctypes.byref(r),
+                                              ctypes.byref(u), ctypes.byref(p)))
+        return {"queued": q.value, "running": r.value, "bytes_used": u.value,
+                "bytes_peak": p.value}
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self._lib.ffr_server_destroy(self._s)
+            self._s = None
 
     def __del__(self):
         try:

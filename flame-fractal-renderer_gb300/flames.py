@@ -15,6 +15,13 @@ every machine.
                      weights Dirichlet(1); bounds [-2,2] x [-1.125,1.125]
   random_3d          the 3-D analogue (2-D variations act on a random plane,
                      given by axis_x / axis_y)
+  batch_jobs         the 256-flame batch: random_2d flames with 2..8 xforms,
+                     square buffers of side log-uniform in [256, 2048],
+                     sample counts log-uniform in [1e7, 1e9]
+  serving_requests   a Poisson request stream: 80% random 2-D flames
+                     (buffers 512..1920 x 512..1080, 1e7..1e9 samples), 15%
+                     random 3-D flames (4..6 xforms, cubes of side 128..384),
+                     5% continuations adding 1e8 samples to a resident buffer
 """
 from __future__ import annotations
 
@@ -108,3 +115,49 @@ def random_3d(seed: int, k: int = 4, size=(256, 256, 256), variations=TIER_A,
         })
     return {"dimensions": 3, "size": list(size),
             "bounds": [[-2.0, 2.0], [-2.0, 2.0], [-2.0, 2.0]], "xforms": xfs}
+
+
+def _log_uniform(g, lo: float, hi: float) -> float:
+    return float(np.exp(g.uniform(np.log(lo), np.log(hi))))
+
+
+def batch_jobs(seed: int = 11, n: int = 256, side=(256, 2048), samples=(1e7, 1e9)):
+    """[(flame, samples)] of the batched-launch workload."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        k = int(g.integers(2, 9))
+        s = int(round(_log_uniform(g, *side)))
+        m = int(round(_log_uniform(g, *samples)))
+        out.append((random_2d(seed * 100_003 + i, k=k, size=(s, s)), m))
+    return out
+
+
+def serving_requests(seed: int = 23, rate: float = 200.0, duration: float = 60.0,
+                     samples=(1e7, 1e9), cont_samples: int = 10**8):
+    """[(arrival_s, kind, flame or None, samples)], kind in {"2d", "3d",
+    "cont"}; arrivals are a Poisson process of `rate` per second."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    t = 0.0
+    i = 0
+    while True:
+        t += float(g.exponential(1.0 / rate))
+        if t >= duration:
+            break
+        u = float(g.uniform())
+        if u < 0.80:
+            w = int(round(_log_uniform(g, 512, 1920)))
+            h = int(round(_log_uniform(g, 512, 1080)))
+            k = int(g.integers(2, 9))
+            out.append((t, "2d", random_2d(seed * 1_000_003 + i, k=k, size=(w, h)),
+                        int(round(_log_uniform(g, *samples)))))
+        elif u < 0.95:
+            c = int(round(_log_uniform(g, 128, 384)))
+            k = int(g.integers(4, 7))
+            out.append((t, "3d", random_3d(seed * 1_000_003 + i, k=k, size=(c, c, c)),
+                        int(round(_log_uniform(g, *samples)))))
+        else:
+            out.append((t, "cont", None, cont_samples))
+        i += 1
+    return out

@@ -191,6 +191,119 @@ ffr_status ffr_batch_render(ffr_batch *b, const uint64_t *samples,
 const char *ffr_batch_last_error(const ffr_batch *b);
 
 /* ---------------------------------------------------------------------
+ * Serving loop: render jobs submitted while others run (continuous
+ * batching), buffers resident on the device.  No reference counterpart: the
+ * reference renders one flame per ffr-buf process (src/ffr_buf.cpp:146-274)
+ * and its -i accumulation reads buffer files back from the host
+ * (src/ffr_buf.cpp:167-183, buffer_renderer.hpp:419-452).
+ *
+ * A job of N samples runs ceil(N / traj_len) streams with one trajectory of
+ * traj_len samples each (the last one shorter), exactly what ffr_render runs
+ * for a context with opts.streams = ceil(N / traj_len) and opts.traj_len =
+ * traj_len, so its counts are identical alone and in any mix of jobs.
+ *
+ * One scheduler thread admits queued jobs in arrival order while the
+ * server's device-memory budget and job slots allow, then runs the admitted
+ * jobs in rounds: one persistent launch per (dims, colour) group over a
+ * slice of every running job's chunks (128 streams each), the slice shared
+ * evenly between running jobs.  Two rounds are in flight at once, so a job
+ * that arrives while others run joins the next round and its work overlaps
+ * theirs on the device.  A job's buffer stays resident after it completes
+ * until every job on it is released; ffr_server_continue adds samples to a
+ * resident buffer (-i accumulation without a host round trip).
+ *
+ * All functions are thread-safe.  Job ids start at 1.
+ * ------------------------------------------------------------------- */
+typedef struct ffr_server ffr_server;
+
+typedef struct ffr_server_opts {
+    uint32_t abi_version;      /* FFR_ABI_VERSION */
+    int32_t device;
+    int32_t precision;         /* ffr_precision, shared by all jobs */
+    int32_t reserved;
+    uint64_t settle;           /* default 53 */
+    uint64_t traj_len;         /* samples per stream; default 4096 */
+    /* device bytes the server may hold: buffers, per-job statistics
+       (about 170 KB each) and a fixed 16 MiB read staging area;
+       0 = free device memory at creation minus 2 GiB */
+    uint64_t hbm_budget;
+    uint64_t max_active;       /* jobs admitted at once; default 256 */
+    uint64_t round_chunks;     /* chunks per round; 0 = twice the resident CTAs */
+    uint64_t timeout_ms;       /* limit of one round's device work; 0 = none */
+} ffr_server_opts;
+
+enum {
+    FFR_JOB_QUEUED = 0,        /* waiting for memory or a slot */
+    FFR_JOB_RUNNING = 1,       /* admitted: buffer resident, chunks running */
+    FFR_JOB_DONE = 2,          /* finished; status FFR_OK or FFR_BAD_VALUES */
+    FFR_JOB_FAILED = 3,        /* status says why */
+    FFR_JOB_CANCELLED = 4
+};
+
+typedef struct ffr_job_info {
+    int32_t state;             /* FFR_JOB_* */
+    int32_t status;            /* ffr_status once finished */
+    uint64_t samples;
+    uint64_t buffer_bytes;     /* size of the buffer in the file layout */
+    uint64_t parent;           /* job whose buffer this one continues, or 0 */
+    uint64_t submit_ns;        /* steady-clock times of submission, */
+    uint64_t admit_ns;         /* admission (0 while queued) */
+    uint64_t done_ns;          /* and completion (0 while unfinished) */
+} ffr_job_info;
+
+void ffr_server_default_opts(ffr_server_opts *opts);
+
+/* Start the scheduler thread on opts->device.  Errors: ffr_last_error(NULL). */
+ffr_status ffr_server_create(const ffr_server_opts *opts, ffr_server **out);
+
+/* Cancel outstanding jobs, wait for in-flight rounds, free everything. */
+void ffr_server_destroy(ffr_server *s);
+
+const char *ffr_server_last_error(const ffr_server *s);
+
+/* Queue a render of `samples` samples of the flame `json` into a new
+   buffer, first adding `init` (the file layout, init_bytes >= the buffer
+   size, or NULL for a zero buffer) as ffr_add_buffer does.  The flame is
+   parsed here (FFR_ERR_PARSE / FFR_ERR_IO come back at once); a buffer
+   larger than the whole budget is FFR_ERR_OOM. */
+ffr_status ffr_server_submit(ffr_server *s, const char *json, size_t len,
+                             const void *init, size_t init_bytes,
+                             uint64_t samples, uint64_t seed, uint64_t bad_limit,
+                             uint64_t *job);
+
+/* Queue `samples` more samples into the buffer of job `parent` (queued,
+   running or finished, not released). */
+ffr_status ffr_server_continue(ffr_server *s, uint64_t parent, uint64_t samples,
+                               uint64_t seed, uint64_t bad_limit, uint64_t *job);
+
+ffr_status ffr_server_poll(ffr_server *s, uint64_t job, ffr_job_info *info);
+
+/* Wait until the job has finished (any terminal state) or timeout_ms has
+   passed (FFR_ERR_TIMEOUT; 0 = no limit).  info may be NULL. */
+ffr_status ffr_server_wait(ffr_server *s, uint64_t job, uint64_t timeout_ms,
+                           ffr_job_info *info);
+
+/* Statistics of a finished job, as ffr_render reports them (kernel_ms is the
+   job's submission-to-completion time). */
+ffr_status ffr_server_job_stats(ffr_server *s, uint64_t job, ffr_stats *st);
+
+/* Copy the job's buffer out in the file layout (its current contents; the
+   final ones once the job and every job continuing it have finished). */
+ffr_status ffr_server_read(ffr_server *s, uint64_t job, void *cells, size_t bytes);
+
+/* Stop a queued or running job (running chunks stop within 4096 samples). */
+ffr_status ffr_server_cancel(ffr_server *s, uint64_t job);
+
+/* Forget a finished job; its buffer is freed once no job refers to it.
+   FFR_ERR_STATE while the job is queued or running. */
+ffr_status ffr_server_release(ffr_server *s, uint64_t job);
+
+/* Current load: queued and running jobs, device bytes held now and at most
+   since creation.  Any pointer may be NULL. */
+ffr_status ffr_server_load(ffr_server *s, uint64_t *queued, uint64_t *running,
+                           uint64_t *bytes_used, uint64_t *bytes_peak);
+
+/* ---------------------------------------------------------------------
  * Verification entry points: the same device code as ffr_render, exposed
  * one function at a time so each can be checked against the reference.
  * ------------------------------------------------------------------- */
