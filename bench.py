@@ -122,6 +122,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def rank_seed(base: int, rank: int) -> int:
+    """Seed of one rank's shard: ranks render disjoint ISAAC streams."""
+    return base + 1_000_003 * rank
+
+
+def rank_totals(kern_ms: float, binned: float, wall: float, dist=None, device="cpu"):
+    """(max device ms, total binned samples, max wall s) over the job's ranks:
+    the whole-job time is the slowest rank's, the work is every rank's."""
+    if dist is None:
+        return kern_ms, float(binned), wall
+    import torch
+    t = torch.tensor([kern_ms, float(binned), wall], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return mx[0].item(), sm[1].item(), mx[2].item()
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -131,13 +150,15 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """Per-launch DRAM traffic of the render kernel from the committed ncu
-    summary (profiles/chaos_fp32_random2d.md), scaled to one launch of the
-    bench's sample count; None when no summary exists."""
+    """Per-launch DRAM traffic (read + write) of the render kernel from the
+    committed ncu summary (profiles/chaos_fp32_random2d.md).  The buffer is
+    L2-resident, so the traffic is the one fill of the buffer after the L2
+    flush and does not depend on the launch's sample count; None when no
+    summary exists."""
     p = os.path.join(ROOT, "profiles", "chaos_fp32_random2d.md")
     try:
         for line in open(p):
-            if line.startswith("dram_bytes_per_binned_sample:"):
+            if line.startswith("dram_bytes_per_launch:"):
                 return float(line.split(":")[1])
     except OSError:
         pass
@@ -332,10 +353,16 @@ def run_tetra3d(args):
         ms, binned, iters, s = _timed_steps(r, args, B, 3)
         clocks = sampler.stop()
         assert r.histogram()[0] == binned
+        import numpy as np
+        occupied = int(np.count_nonzero(r.counts()))
     value = binned / (ms * 1e-3)
     peaks, kind = measured_peaks()
     achieved = 8.0 * binned / (ms * 1e-3) / 1e9
-    atom = ffr.measure_atomic_rate(512 ** 3, 1 << 31, device=dev)
+    # the hits land on the attractor's occupied cells only: the matching
+    # peak is the atomic rate over a buffer of that many cells (L2-resident),
+    # not over the whole 512^3 buffer (HBM-bound)
+    atom = ffr.measure_atomic_rate(occupied, 1 << 31, device=dev)
+    atom_full = ffr.measure_atomic_rate(512 ** 3, 1 << 31, device=dev)
     tv = None if args.no_tv else tv_check(ffr, text, 10**8, settle, dev)
     _line(args, "Sierpinski tetrahedron, 512^3 u32 buffer, 1e10 samples", value,
           ms / args.steps, "f32",
@@ -347,7 +374,9 @@ def run_tetra3d(args):
                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
                     "peak_source": kind},
           l2_atomic={"peak_ops_per_s": atom, "achieved_ops_per_s": value, "frac": value / atom,
-                     "what": "u32 atomic adds at uniformly random cells of a 512^3 buffer"},
+                     "what": f"u32 atomic adds at uniformly random cells of a buffer of "
+                             f"{occupied} cells (the occupied cells of the 512^3 buffer)",
+                     "whole_buffer_peak_ops_per_s": atom_full},
           tv=tv, clocks=clocks, iterated_per_s=iters / (ms * 1e-3))
 
 
@@ -547,6 +576,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--max-active", type=int, default=256)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted"],
+                    help="render kernel (auto: the library's autotuner decides)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -571,7 +602,7 @@ def main():
     prec = ffr.FP32 if args.precision == "fp32" else ffr.FP64
     B = int(args.samples_per_step)
     settle = 20
-    seed_base = 7 + 1_000_003 * rank
+    seed_base = rank_seed(7, rank)
 
     def barrier():
         torch.cuda.synchronize()
@@ -579,7 +610,9 @@ def main():
             dist.barrier()
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    r = ffr.BufferRenderer(text, precision=prec, settle=settle, device=local)
+    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED}
+    r = ffr.BufferRenderer(text, precision=prec, settle=settle, device=local,
+                           kernel=kern[args.kernel])
     for w in range(args.warmup):
         r.render(B, seed_base + 10_000 + w)
     r.clear()
@@ -607,15 +640,8 @@ def main():
     hsum = r.histogram()[0]
     assert hsum == binned, (hsum, binned)
     # max over ranks of the device time; whole-job binned = sum over ranks
-    t = torch.tensor([kern_ms, float(binned), wall], dtype=torch.float64, device=f"cuda:{local}")
-    if dist:
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        kern_ms_all, binned_all, wall_all = mx[0].item(), sm[1].item(), mx[2].item()
-    else:
-        kern_ms_all, binned_all, wall_all = kern_ms, float(binned), wall
+    kern_ms_all, binned_all, wall_all = rank_totals(kern_ms, binned, wall, dist,
+                                                    device=f"cuda:{local}")
     value = binned_all / (kern_ms_all * 1e-3)
     r.close()
 
@@ -628,7 +654,8 @@ def main():
     barrier()
     te = time.perf_counter()
     for k in range(e2e_steps):
-        with ffr.BufferRenderer(text, precision=prec, settle=settle, device=local) as er:
+        with ffr.BufferRenderer(text, precision=prec, settle=settle, device=local,
+                                kernel=kern[args.kernel]) as er:
             if pinned is None:
                 pinned = torch.empty(er.buffer_bytes, dtype=torch.uint8).pin_memory()
             s = er.render(B, seed_base + 500 + k)
@@ -650,10 +677,9 @@ def main():
     per_launch_bytes = 8.0 * binned / launches
     avg_s = kern_ms / launches * 1e-3
     achieved = per_launch_bytes / avg_s / 1e9
-    dram_per_sample = profile_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                "traffic": (dram_per_sample * binned / launches) if dram_per_sample else None,
+                "traffic": profile_traffic(),
                 "peak_source": peak_kind,
                 "kernel": f"render kernel ({kernel_used}), FP32"}
     atom = ffr.measure_atomic_rate(1920 * 1080, 1 << 31, device=local)

@@ -1,4 +1,4 @@
-"""Build libffr_gpu.so and the ffr-buf executable in-tree.
+"""Build libffr_gpu.so and the ffr-buf / ffr-img executables in-tree.
 
 Outputs go to flame-fractal-renderer_gb300/_build/ (git-ignored).  Every
 CUDA translation unit is compiled for sm_103a only; the six chaos-kernel
@@ -22,6 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libffr_gpu.so")
 CLI = os.path.join(OUT, "ffr-buf")
+IMG_CLI = os.path.join(OUT, "ffr-img")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -77,11 +78,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 jobs.append((obj, [src] + hdrs,
                              [nvcc, *nv_common, *extra, f"-DFFR_P={p}", f"-DFFR_D={d}",
                               f"-DFFR_KIND={kind}", "-c", src, "-o", obj]))
-    for name in ("buffer_kernels", "noalloc"):
+    for name in ("buffer_kernels", "image_kernels", "noalloc"):
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
-    for name in ("api", "server", "flame", "json", "variations_host"):
+    for name in ("api", "server", "png", "flame", "json", "variations_host"):
         src = os.path.join(CSRC, name + ".cpp")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [*cxx_common, "-c", src, "-o", obj]))
@@ -99,12 +100,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs,
               "-Xlinker", f"--version-script={exports}", "-lpthread", "-ldl", "-lrt"])
         os.replace(tmp, LIB)
-    cli_src = os.path.join(CSRC, "ffr_buf_cli.cpp")
-    if force or _stale(CLI, [cli_src, LIB, os.path.join(INCLUDE, "ffr_gpu.h")]):
-        tmp = CLI + f".tmp{os.getpid()}"
-        _run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", INCLUDE, cli_src,
-              "-o", tmp, "-L", OUT, "-lffr_gpu", "-Wl,-rpath,$ORIGIN"])
-        os.replace(tmp, CLI)
+    for exe, src in ((CLI, "ffr_buf_cli.cpp"), (IMG_CLI, "ffr_img_cli.cpp")):
+        cli_src = os.path.join(CSRC, src)
+        if force or _stale(exe, [cli_src, LIB, os.path.join(INCLUDE, "ffr_gpu.h")]):
+            tmp = exe + f".tmp{os.getpid()}"
+            _run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", INCLUDE, cli_src,
+                  "-o", tmp, "-L", OUT, "-lffr_gpu", "-Wl,-rpath,$ORIGIN"])
+            os.replace(tmp, exe)
     if verbose:
         print(f"built {LIB} and {CLI}", file=sys.stderr)
     return LIB

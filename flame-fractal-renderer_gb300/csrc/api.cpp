@@ -480,7 +480,14 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
         return FFR_OK;
     const size_t cells = c->flame.cells;
     const size_t r = (size_t)c->flame.color_dims;
-    const size_t need = cells * 4 * (spill ? 2 : 1) + cells * r * 8 + sizeof(DevStats);
+    // scratch: counts | high words | colours | statistics, each 256-byte
+    // aligned (an odd cell count would otherwise leave the u64 fields of
+    // the statistics on a 4-byte boundary)
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t off_hi = up(cells * 4);
+    const size_t off_col = off_hi + (spill ? up(cells * 4) : 0);
+    const size_t off_st = off_col + up(cells * r * 8);
+    const size_t need = off_st + sizeof(DevStats);
     size_t fr = 0, tot = 0;
     CU(c, cudaMemGetInfo(&fr, &tot));
     if (need > fr / 4)
@@ -488,9 +495,9 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
     unsigned char* buf = nullptr;
     CU(c, cudaMalloc(&buf, need));
     unsigned int* pc = reinterpret_cast<unsigned int*>(buf);
-    unsigned int* ph = spill ? pc + cells : nullptr;
-    double* pcol = r ? reinterpret_cast<double*>(buf + cells * 4 * (spill ? 2 : 1)) : nullptr;
-    DevStats* pst = reinterpret_cast<DevStats*>(buf + cells * 4 * (spill ? 2 : 1) + cells * r * 8);
+    unsigned int* ph = spill ? reinterpret_cast<unsigned int*>(buf + off_hi) : nullptr;
+    double* pcol = r ? reinterpret_cast<double*>(buf + off_col) : nullptr;
+    DevStats* pst = reinterpret_cast<DevStats*>(buf + off_st);
     const uint64_t P = std::min<uint64_t>(samples, c->opts.precision == FFR_FP64 ? (1u << 22)
                                                                                  : (1u << 24));
     float best = 1e30f;
@@ -895,6 +902,57 @@ ffr_status ffr_histogram(ffr_ctx* c, uint64_t* sum, uint64_t* mn, uint64_t* mx)
     if (mn) *mn = out[1];
     if (mx) *mx = out[2];
     return FFR_OK;
+}
+
+ffr_status ffr_render_image(ffr_ctx* c, int mode, double gamma, uint32_t bits, void* pixels,
+                            size_t bytes, ffr_image_info* info)
+{
+    if (!c)
+        return FFR_ERR_ARG;
+    if (c->flame.dims != 2)
+        return fail(c, FFR_ERR_ARG, "only 2D flames supported");
+    if (mode < FFR_IMAGE_MONO || mode > FFR_IMAGE_RGB)
+        return fail(c, FFR_ERR_ARG, "no coloring flag");
+    // ffr_img.cpp:89-95
+    if (!(gamma >= 1e-20))
+        return fail(c, FFR_ERR_ARG, "gamma too small");
+    if (bits != 8 && bits != 16)
+        return fail(c, FFR_ERR_ARG, "bits per channel must be 8 or 16");
+    if (mode == FFR_IMAGE_MONO)
+        bits = 8;       // the reference writes monochrome as an 8-bit gray image
+    if (mode == FFR_IMAGE_RGB && c->flame.color_dims != 3)
+        return fail(c, FFR_ERR_ARG, "buffer must use 3 color dimensions");
+    const uint32_t ch = mode == FFR_IMAGE_RGB ? 3 : 1;
+    const size_t need = (size_t)c->flame.cells * ch * (bits / 8);
+    if (!pixels || bytes < need)
+        return fail(c, FFR_ERR_IO, "error writing output: destination too small");
+    uint64_t sum = 0, mn = 0, mx = 0;
+    ffr_status s = ffr_histogram(c, &sum, &mn, &mx);
+    if (s != FFR_OK)
+        return s;
+    // max of log(1 + count) over the cells is log(1 + max count): log is
+    // monotone, and the host's libm gives the reference's value
+    const double smin = std::log(1.0 + (double)mn), smax = std::log(1.0 + (double)mx);
+    if (info)
+    {
+        info->hist_min = mn;
+        info->hist_max = mx;
+        info->scale_min = smin;
+        info->scale_max = smax;
+        info->width = (uint32_t)c->flame.size[0];
+        info->height = (uint32_t)c->flame.size[1];
+        info->channels = ch;
+        info->bits = bits;
+    }
+    if (smax < 1e-20)
+        return fail(c, FFR_ERR_STATE, "histogram is (probably) empty");
+    CU(c, cudaSetDevice(c->device));
+    if ((s = ensure_scratch(c, need + 64)) != FFR_OK)
+        return s;
+    CU(c, launch_image(c->d_scratch, (int)bits, c->flame.cells, mode, c->flame.color_dims,
+                       c->d_counts, c->d_hi, c->d_colors, smax, 1.0 / gamma, c->stream));
+    CU(c, cudaMemcpyAsync(pixels, c->d_scratch, need, cudaMemcpyDeviceToHost, c->stream));
+    return wait_stream(c);
 }
 
 ffr_status ffr_clear(ffr_ctx* c)

@@ -111,15 +111,24 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     }
 }
 
+// first i with m <= thresh[i]: the thresholds of the first nxf-1 xforms are
+// non-decreasing (prefix sums of non-negative weights) and the last is 2^53,
+// so the index is the number of leading thresholds below m.  A fixed-trip
+// count instead of a search loop: lanes do not diverge on it.
+__device__ __forceinline__ int pick_branchless(const uint64_t* thresh, int nxf, uint64_t m)
+{
+    int x = 0;
+#pragma unroll 4
+    for (int i = 0; i < nxf - 1; ++i)
+        x += m > thresh[i] ? 1 : 0;
+    return x;
+}
+
 // Flame::getRandomXForm via exact integer thresholds (flame_program.h)
 template <typename R, typename Rng>
-__device__ __forceinline__ int pick_xform(const Prog<R>& pg, Rng& rng)
+__device__ __forceinline__ int pick_xform(const Prog<R>& pg, int nxf, Rng& rng)
 {
-    const uint64_t m = rng.next() >> 11;
-    int i = 0;
-    while (m > pg.thresh[i])
-        ++i;
-    return i;
+    return pick_branchless(pg.thresh, nxf, rng.next() >> 11);
 }
 
 template <int D, typename R>
@@ -191,7 +200,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     const ProgHeader<R>& h = *pg.h;
     const int nxf = a.nxf;
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
-    uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + 2 * 16 * BLOCK);
+    uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + (16 + kIsaacRslWords) * BLOCK);
     unsigned long long* xfc_shared = reinterpret_cast<unsigned long long*>(xfc_local);
     const bool local_xfc = nxf <= kLocalXfCounters;
     if (local_xfc)
@@ -206,9 +215,17 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
         __syncthreads();
     }
 
-    DevIsaac<BLOCK> rng;
+    DevIsaac<BLOCK, kIsaacRslWords> rng;
     rng.mem = ismem + threadIdx.x;
     rng.rsl = ismem + 16 * BLOCK + threadIdx.x;
+    // words one sample step can draw: the choice, the chosen xform's
+    // variations, the final xform's
+    const unsigned int low = 1u + h.rng_words_max + (h.has_final ? pg.xf[nxf].rng_words : 0u);
+    // refill ahead, warp-uniformly, once some lane could run dry this step
+    auto refill_ahead = [&]() __attribute__((always_inline)) {
+        if (__any_sync(__activemask(), rng.cnt < low) && rng.cnt <= kIsaacRslWords - 16)
+            rng.refill();
+    };
 
     unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
     R ext_lo[D], ext_hi[D];
@@ -243,14 +260,16 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 break;
             }
             R p[D], pf[D];
-            // RenderIterator::_init (render_iterator.hpp:52-60)
-            auto init = [&]() {
+            // RenderIterator::_init (render_iterator.hpp:52-60); inlined so
+            // the trajectory state stays in registers
+            auto init = [&]() __attribute__((always_inline)) {
 #pragma unroll
                 for (int i = 0; i < D; ++i)
                     p[i] = R(2) * T::unit(rng.next()) - R(1);
                 for (unsigned long long k = 0; k < a.settle; ++k)
                 {
-                    const int xi = pick_xform<R>(pg, rng);
+                    refill_ahead();
+                    const int xi = pick_xform<R>(pg, nxf, rng);
                     R q[D];
                     apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
 #pragma unroll
@@ -265,7 +284,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
             unsigned int poll = 0;
             for (; len > 0; --len)
             {
-                const int xi = pick_xform<R>(pg, rng);
+                refill_ahead();
+                const int xi = pick_xform<R>(pg, nxf, rng);
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
@@ -569,14 +589,14 @@ __global__ void trace_kernel(const TraceArgs a)
     for (unsigned long long k = 0; k < a.settle; ++k)
     {
         R q[D];
-        apply_xform<D, R>(pg, pg.xf[pick_xform<R>(pg, rng)], p, q, rng);
+        apply_xform<D, R>(pg, pg.xf[pick_xform<R>(pg, pg.h->nxf, rng)], p, q, rng);
 #pragma unroll
         for (int i = 0; i < D; ++i)
             p[i] = q[i];
     }
     for (unsigned long long k = 0; k < a.n; ++k)
     {
-        const int xi = pick_xform<R>(pg, rng);
+        const int xi = pick_xform<R>(pg, pg.h->nxf, rng);
         R q[D];
         apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
 #pragma unroll

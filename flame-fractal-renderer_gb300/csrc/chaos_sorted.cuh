@@ -145,18 +145,6 @@ struct PreDrawn
     __device__ __forceinline__ uint64_t next() { return w[(k++) * T]; }
 };
 
-// first i with m <= thresh[i]: the thresholds of the first nxf-1 xforms are
-// non-decreasing (prefix sums of non-negative weights) and the last is 2^53,
-// so the index is the number of leading thresholds below m
-__device__ __forceinline__ int pick_branchless(const uint64_t* thresh, int nxf, uint64_t m)
-{
-    int x = 0;
-#pragma unroll 4
-    for (int i = 0; i < nxf - 1; ++i)
-        x += m > thresh[i] ? 1 : 0;
-    return x;
-}
-
 template <int D, typename R, bool COLOR, int T>
 __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* smem)
 {

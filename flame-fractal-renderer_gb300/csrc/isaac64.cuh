@@ -10,10 +10,19 @@
 //          16 words for every seed (the golden-ratio mix, computed once on
 //          the host: isaac_init_table()), and only a, b, c carry the seed.
 //
-// GB300 layout: the two 16-word arrays of each thread live in shared memory
-// as [word][thread] (stride BLOCK).  gen() indexes randmem with
-// data-dependent words; with this layout lane L always hits bank pair
-// (2L mod 32) whatever the word index, so every access is conflict-free.
+// GB300 layout: randmem (16 words) and the result array (CAP words) of each
+// thread live in shared memory as [word][thread] (stride BLOCK).  gen()
+// indexes randmem with data-dependent words; with this layout lane L always
+// hits bank pair (2L mod 32) whatever the word index, so every access is
+// conflict-free.
+//
+// Refill ahead (CAP > 16): refill() moves the cnt unconsumed words up to
+// rsl[16..16+cnt) and generates the next block into rsl[0..16); next() keeps
+// consuming downwards, so the word sequence is exactly Isaac::next's, only
+// the moment of generation moves earlier.  A warp can then regenerate all
+// its lanes at one point (one masked gen() for the warp) instead of running
+// gen() at every step for the few lanes that happen to run dry, which is
+// what happens once lanes draw different numbers of words per step.
 #pragma once
 
 #include <cstdint>
@@ -40,11 +49,12 @@ __host__ __device__ inline uint64_t stream_key(uint64_t seed, uint64_t stream)
 }
 
 #ifdef __CUDACC__
-template <int BLOCK>
+template <int BLOCK, int CAP = 16>
 struct DevIsaac
 {
-    uint64_t* mem;      // &smem_mem[threadIdx.x], stride BLOCK
-    uint64_t* rsl;      // &smem_rsl[threadIdx.x], stride BLOCK
+    static_assert(CAP >= 16, "the result array holds at least one block");
+    uint64_t* mem;      // &smem_mem[threadIdx.x], stride BLOCK, 16 words
+    uint64_t* rsl;      // &smem_rsl[threadIdx.x], stride BLOCK, CAP words
     uint64_t a, b, c;
     uint32_t cnt;
 
@@ -102,6 +112,16 @@ struct DevIsaac
         }
         --cnt;
         return Rs((int)cnt);
+    }
+
+    // generate the next block now, keeping the cnt unconsumed words (needs
+    // cnt <= CAP - 16)
+    __device__ __forceinline__ void refill()
+    {
+        for (int k = (int)cnt - 1; k >= 0; --k)
+            Rs(16 + k) = Rs(k);
+        gen();
+        cnt += 16;
     }
 };
 #endif // __CUDACC__

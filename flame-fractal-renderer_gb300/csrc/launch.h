@@ -54,17 +54,21 @@ struct RenderArgs
 };
 
 constexpr int kLocalXfCounters = 16;
+// ISAAC result array per render thread: one block plus a full block of
+// words carried across a refill-ahead (isaac64.cuh)
+constexpr int kIsaacRslWords = 32;
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
 
 // Dynamic shared memory of the plain and batch render kernels: the program,
-// ISAAC state [16][BLOCK] x2, and per-thread u32 xform counters when
-// nxf <= kLocalXfCounters, else one u64 counter per xform for the CTA.
+// ISAAC state (randmem [16][BLOCK], results [kIsaacRslWords][BLOCK]), and
+// per-thread u32 xform counters when nxf <= kLocalXfCounters, else one u64
+// counter per xform for the CTA.
 template <int BLOCK>
 __host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf)
 {
     size_t s = align16u(prog_bytes);
-    s += 2 * 16 * (size_t)BLOCK * sizeof(uint64_t);
+    s += (16 + kIsaacRslWords) * (size_t)BLOCK * sizeof(uint64_t);
     if (nxf <= kLocalXfCounters)
         s += (size_t)nxf * BLOCK * sizeof(uint32_t);
     else
@@ -212,6 +216,11 @@ cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned i
 // zero the statistics of every job (one CTA per job) and the batch cursor
 cudaError_t launch_batch_reset(const JobDesc* jobs, int njobs, BatchHead* head,
                                cudaStream_t);
+
+// image_kernels.cu: ffr-img's pixel mapping (mode 0 mono, 1 gray, 2 RGB)
+cudaError_t launch_image(void* out, int bits, unsigned long long cells, int mode,
+                         int color_dims, const unsigned int* counts, const unsigned int* hi,
+                         const double* colors, double max_l, double gp, cudaStream_t st);
 
 // zero one statistics block (nxf per-xform counters), extremes to +/-inf
 cudaError_t launch_stats_reset(DevStats* st, int nxf, cudaStream_t);

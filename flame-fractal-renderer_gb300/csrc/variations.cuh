@@ -203,6 +203,90 @@ __device__ __forceinline__ void rand_dir(Rng& rng, R* d)
     }
 }
 
+// The seven variations of the benchmark flames (linear, sinusoidal,
+// spherical, swirl, horseshoe, polar, julia).
+constexpr uint64_t kTierAMask = (1ull << V_LINEAR) | (1ull << V_SINUSOIDAL)
+    | (1ull << V_SPHERICAL) | (1ull << V_SWIRL) | (1ull << V_HORSESHOE) | (1ull << V_POLAR)
+    | (1ull << V_JULIA);
+
+__host__ __device__ inline bool tier_a(int type)
+{
+    return type >= 0 && type < 64 && ((kTierAMask >> type) & 1ull);
+}
+
+// The seven benchmark variations with their shared primitives merged.  In a
+// warp whose lanes apply different variations, the 98-way switch runs one
+// body per distinct type; here sqrt(r^2) is computed once for horseshoe,
+// polar and julia lanes, atan2 once for polar and julia lanes, and one
+// sincos serves swirl (of r^2) and julia (of the half angle), so a warp pays
+// each primitive at most once.  Every type still evaluates exactly the
+// expression of its case below, in the same operation order (the FP64
+// results are bit-identical to the switch), and julia draws its word at the
+// same point of the RNG sequence.
+template <int D, typename R, typename Rng>
+__device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R* out, Rng& rng)
+{
+    using T = RealTraits<R>;
+    const int ty = v.type;
+    if (ty < kFirst2D)
+    {
+        if (ty == V_SINUSOIDAL)     /* 183-191 */
+        {
+            for (int i = 0; i < D; ++i) out[i] = T::sin_(t[i]);
+        }
+        else if (ty == V_SPHERICAL) /* 197-208 */
+        {
+            const R r = T::recip_(nsq<D>(t) + T::eps);
+            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
+        }
+        else                        /* 169-177 linear */
+        {
+            for (int i = 0; i < D; ++i) out[i] = t[i];
+        }
+        return;
+    }
+    const int ax = v.axis_x, ay = v.axis_y;
+    const R x = coord<D>(t, ax), y = coord<D>(t, ay);
+    const R q = x * x + y * y;
+    const bool is_swirl = ty == V_SWIRL, is_julia = ty == V_JULIA;
+    R rt = R(0), ang = R(0), s = R(0), c = R(0);
+    if (!is_swirl)                  // horseshoe, polar, julia: sqrt(x^2 + y^2)
+        rt = T::sqrt_(q);
+    if (ty == V_POLAR || is_julia)  // atan2(y, x)
+        ang = T::atan2_(y, x);
+    if (is_swirl || is_julia)
+    {
+        R arg = q;                  /* swirl 509-522: sincos(r^2) */
+        if (is_julia)               /* julia 807-819: a/2 + pi * randBool */
+            arg = R(0.5) * ang + (R)(rng.next() & 1u) * T::pi;
+        T::sincos_(arg, &s, &c);
+    }
+    R X, Y;
+    if (is_swirl)
+    {
+        X = x * s - y * c;
+        Y = x * c + y * s;
+    }
+    else if (ty == V_HORSESHOE)     /* 527-540 */
+    {
+        const R r = T::recip_(rt + T::eps);
+        X = ((x - y) * (x + y)) * r;
+        Y = (R(2.0) * x * y) * r;
+    }
+    else if (ty == V_POLAR)         /* 545-555 */
+    {
+        X = ang * T::inv_pi;
+        Y = rt - R(1.0);
+    }
+    else                            /* julia */
+    {
+        X = c * rt;
+        Y = s * rt;
+    }
+    for (int i = 0; i < D; ++i)
+        out[i] = i == ax ? X : (i == ay ? Y : R(0));
+}
+
 // one variation: o = V(t).  Restates each class of
 // src/variations/variations.hpp (line numbers in the case comments) in the
 // reference's operation order; Point / k is multiplication by (1/k), as
@@ -213,6 +297,11 @@ template <int D, typename R, typename Rng>
 __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng)
 {
     using T = RealTraits<R>;
+    if (tier_a(v.type))
+    {
+        variation_tier_a<D, R>(v, t, o, rng);
+        return;
+    }
     const int ax = v.axis_x, ay = v.axis_y;
     R* out = o;
 

@@ -45,7 +45,10 @@ EXPORTS = [
     "ffr_server_last_error", "ffr_server_submit", "ffr_server_continue",
     "ffr_server_poll", "ffr_server_wait", "ffr_server_job_stats", "ffr_server_read",
     "ffr_server_cancel", "ffr_server_release", "ffr_server_load",
+    "ffr_render_image", "ffr_encode_png",
 ]
+IMG_CLI_PATH = os.path.join(HERE, "_build", "ffr-img")
+IMAGE_MONO, IMAGE_GRAY, IMAGE_RGB = 0, 1, 2
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
 
@@ -78,6 +81,13 @@ class Stats(ctypes.Structure):
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
                 ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32)]
+
+
+class ImageInfo(ctypes.Structure):
+    _fields_ = [("hist_min", ctypes.c_uint64), ("hist_max", ctypes.c_uint64),
+                ("scale_min", ctypes.c_double), ("scale_max", ctypes.c_double),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("channels", ctypes.c_uint32), ("bits", ctypes.c_uint32)]
 
 
 class ServerOpts(ctypes.Structure):
@@ -161,6 +171,10 @@ def load_library(path: str = LIB_PATH):
         L.ffr_server_cancel.argtypes = [vp, u64]
         L.ffr_server_release.argtypes = [vp, u64]
         L.ffr_server_load.argtypes = [vp, P(u64), P(u64), P(u64), P(u64)]
+        L.ffr_render_image.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint32,
+                                       vp, sz, P(ImageInfo)]
+        L.ffr_encode_png.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_uint32, vp, sz, P(sz)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is ctypes.c_int:      # default: ffr_status
@@ -329,6 +343,18 @@ class BufferRenderer:
     def clear(self) -> None:
         _check(self._lib, self._ctx, self._lib.ffr_clear(self._ctx))
 
+    def render_image(self, mode: int = IMAGE_GRAY, gamma: float = 1.0, bits: int = 8):
+        """ffr-img's pixels of the buffer: (array [height, width(, 3)], info)."""
+        pbits = 8 if mode == IMAGE_MONO else bits
+        ch = 3 if mode == IMAGE_RGB else 1
+        dt = np.uint8 if pbits == 8 else np.uint16
+        w, h = self.size[0], self.size[1] if self.dims > 1 else 1
+        out = np.zeros((h, w, ch), dtype=dt)
+        info = ImageInfo()
+        _check(self._lib, self._ctx, self._lib.ffr_render_image(
+            self._ctx, mode, gamma, bits, _ptr(out), out.nbytes, ctypes.byref(info)))
+        return (out if ch == 3 else out[:, :, 0]), info
+
     def step(self, xf_index: int, key: int, pts: np.ndarray) -> np.ndarray:
         pts = np.ascontiguousarray(pts, dtype=np.float64)
         out = np.zeros_like(pts)
@@ -342,6 +368,22 @@ class BufferRenderer:
         _check(self._lib, self._ctx, self._lib.ffr_trace(self._ctx, key, settle, n,
                                                          _ptr(ids), _ptr(pts)))
         return ids, pts
+
+
+def encode_png(pixels: np.ndarray) -> bytes:
+    """PNG file bytes of a [h, w] or [h, w, 3] u8/u16 array (ffr_encode_png)."""
+    lib = load_library()
+    a = np.ascontiguousarray(pixels)
+    h, w = a.shape[0], a.shape[1]
+    ch = 3 if a.ndim == 3 else 1
+    bits = 8 * a.dtype.itemsize
+    n = ctypes.c_size_t()
+    lib.ffr_encode_png(_ptr(a), w, h, ch, bits, None, 0, ctypes.byref(n))
+    out = np.zeros(n.value, dtype=np.uint8)
+    st = lib.ffr_encode_png(_ptr(a), w, h, ch, bits, _ptr(out), out.nbytes, ctypes.byref(n))
+    if st != FFR_OK:
+        raise FfrError(st, "ffr_encode_png failed")
+    return out.tobytes()
 
 
 def create_status(flame_text: str, precision: int = FP64):

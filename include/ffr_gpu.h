@@ -164,6 +164,41 @@ ffr_status ffr_histogram(ffr_ctx *ctx, uint64_t *sum, uint64_t *min,
 ffr_status ffr_clear(ffr_ctx *ctx);
 
 /* ---------------------------------------------------------------------
+ * Image output (the ffr-img side of the reference): buffer -> pixels on the
+ * device, pixels -> PNG on the host.
+ * ------------------------------------------------------------------- */
+enum { FFR_IMAGE_MONO = 0, FFR_IMAGE_GRAY = 1, FFR_IMAGE_RGB = 2 };
+
+typedef struct ffr_image_info {
+    uint64_t hist_min, hist_max;    /* "histogram bounds" (ffr_img.cpp:212-218) */
+    double scale_min, scale_max;    /* "scaler bounds": log(1 + count) */
+    uint32_t width, height;         /* flame size x, y */
+    uint32_t channels;              /* 1 (mono, gray) or 3 (RGB) */
+    uint32_t bits;                  /* 8 or 16 per channel */
+} ffr_image_info;
+
+/* ffr-img's pixel mapping of the context's 2-D buffer (render_image,
+   src/ffr_img.cpp:199-309; ImageRenderer::renderGrayImage /
+   renderColorImageRGB, src/renderers/image_renderer.hpp:139-191):
+   mode FFR_IMAGE_MONO (count != 0, always 8 bits), FFR_IMAGE_GRAY
+   (pow(log(1 + count) / max, 1/gamma)) or FFR_IMAGE_RGB (the gray level
+   times the mean of the 3 colour dimensions).  pixels receives width x height
+   pixels of `channels` native-endian u8/u16 samples, row y at offset y*width
+   (the buffer's order).  Errors as the reference: non-2-D flame, gamma below
+   1e-20, bits other than 8/16, RGB without 3 colour dimensions (FFR_ERR_ARG);
+   an empty histogram (FFR_ERR_STATE). */
+ffr_status ffr_render_image(ffr_ctx *ctx, int mode, double gamma, uint32_t bits,
+                            void *pixels, size_t bytes, ffr_image_info *info);
+
+/* PNG file bytes of 8- or 16-bit gray (channels 1) or RGB (channels 3)
+   pixels (writePng, src/utils/image.cpp:9-16; uncompressed deflate blocks).
+   *len receives the file size; when cap is smaller (or out is NULL) nothing
+   is written and the call returns FFR_ERR_IO. */
+ffr_status ffr_encode_png(const void *pixels, uint32_t width, uint32_t height,
+                          uint32_t channels, uint32_t bits, void *out, size_t cap,
+                          size_t *len);
+
+/* ---------------------------------------------------------------------
  * Batched render: many flames (contexts on one device, one precision) in
  * one persistent launch per (dims, colour) group, replayed from a captured
  * CUDA graph.  No single reference counterpart: it runs, for every context,

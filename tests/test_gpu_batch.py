@@ -105,3 +105,24 @@ def test_batch_many_flames(ffr, flames):
     assert all(st.samples_iterated == n for st, n in zip(sts, ns))
     for r in rs:
         r.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_autotuned_render_with_odd_cell_count(ffr, flames, precision):
+    """Renders of 2^25 samples or more are autotuned on a scratch copy of the
+    buffer.  With an odd cell count the scratch's statistics block must still
+    start 8-byte aligned (its u64 atomics need it), and the autotuned render
+    equals a render with the kernel fixed."""
+    text = json.dumps(flames.random_2d(11, k=4, size=(723, 723)))
+    n = 1 << 25
+    S = n // 4096
+    with ffr.BufferRenderer(text, precision=precision, settle=20, traj_len=4096,
+                            streams=S) as a:
+        sa = a.render(n, 5, bad_limit=10**9)
+        got = a.counts()
+    with ffr.BufferRenderer(text, precision=precision, settle=20, traj_len=4096,
+                            streams=S, kernel=ffr.KERNEL_PLAIN) as b:
+        sb = b.render(n, 5, bad_limit=10**9)
+        want = b.counts()
+    np.testing.assert_array_equal(got, want)
+    assert sa.samples_plotted == sb.samples_plotted
