@@ -543,6 +543,24 @@ def run_serving(args):
     kinds = {}
     for r in results:
         kinds.setdefault(r[0], []).append((r[2] - r[1]) * 1e-6)
+    # TV of served FP32 results against FP64: a served job's buffer equals the
+    # solo FP32 render with streams = ceil(N / 4096) (tests/test_gpu_server.py),
+    # so four 2-D requests of at most 2e8 samples are re-rendered that way
+    tvs = []
+    if not args.no_tv:
+        picks = [i for i, (_, k, _, n) in enumerate(reqs) if k == "2d" and n <= 2 * 10**8][:4]
+        for i in picks:
+            n = reqs[i][3]
+            hs = []
+            for prec, seed in ((ffr.FP32, 50_000 + i), (ffr.FP64, 7_000 + i), (ffr.FP64, 8_000 + i)):
+                with ffr.BufferRenderer(texts[i], precision=prec, settle=20, traj_len=4096,
+                                        streams=-(-n // 4096), device=dev) as r:
+                    r.render(n, seed, bad_limit=10**12)
+                    hs.append(r.counts())
+            floor = tv_distance(hs[1], hs[2])
+            d = tv_distance(hs[0], hs[1])
+            tvs.append({"request": i, "samples": n, "fp32_vs_fp64": d, "fp64_noise_floor": floor,
+                        "ratio": d / floor if floor > 0 else None})
     _line(args, f"Poisson serving stream, {args.rate:g} req/s for {args.duration:g} s "
           "(80% 2-D, 15% 3-D, 5% continuations)", binned / span, span * 1e3, "f32",
           {"requests": len(reqs), "completed": len(results), "rate_per_s": args.rate,
@@ -554,6 +572,8 @@ def run_serving(args):
                       "by_kind_p50": {k: float(np.percentile(v, 50)) for k, v in kinds.items()},
                       "by_kind_p99": {k: float(np.percentile(v, 99)) for k, v in kinds.items()}},
           offered_samples_per_s=offered, iterated_per_s=iters / span, wall_s=wall,
+          tv={"served_jobs": tvs,
+              "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
           statuses=sorted({r[6] for r in results}), errors=errors[:5],
           server_load=load, clocks=clocks)
 

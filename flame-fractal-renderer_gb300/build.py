@@ -1,4 +1,4 @@
-"""Build libffr_gpu.so and the ffr-buf / ffr-img executables in-tree.
+"""Build libffr_gpu.so and the ffr-buf / ffr-img / ffr-serve executables in-tree.
 
 Outputs go to flame-fractal-renderer_gb300/_build/ (git-ignored).  Every
 CUDA translation unit is compiled for sm_103a only; the six chaos-kernel
@@ -23,6 +23,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libffr_gpu.so")
 CLI = os.path.join(OUT, "ffr-buf")
 IMG_CLI = os.path.join(OUT, "ffr-img")
+SERVE_CLI = os.path.join(OUT, "ffr-serve")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -100,12 +101,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs,
               "-Xlinker", f"--version-script={exports}", "-lpthread", "-ldl", "-lrt"])
         os.replace(tmp, LIB)
-    for exe, src in ((CLI, "ffr_buf_cli.cpp"), (IMG_CLI, "ffr_img_cli.cpp")):
+    for exe, src in ((CLI, "ffr_buf_cli.cpp"), (IMG_CLI, "ffr_img_cli.cpp"),
+                     (SERVE_CLI, "ffr_serve_cli.cpp")):
         cli_src = os.path.join(CSRC, src)
-        if force or _stale(exe, [cli_src, LIB, os.path.join(INCLUDE, "ffr_gpu.h")]):
+        if force or _stale(exe, [cli_src, LIB, os.path.join(INCLUDE, "ffr_gpu.h"),
+                                 os.path.join(INCLUDE, "ffr_wire.h")]):
             tmp = exe + f".tmp{os.getpid()}"
             _run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", INCLUDE, cli_src,
-                  "-o", tmp, "-L", OUT, "-lffr_gpu", "-Wl,-rpath,$ORIGIN"])
+                  "-o", tmp, "-L", OUT, "-lffr_gpu", "-lpthread", "-Wl,-rpath,$ORIGIN"])
             os.replace(tmp, exe)
     if verbose:
         print(f"built {LIB} and {CLI}", file=sys.stderr)

@@ -284,7 +284,8 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
             k = FFR_KERNEL_PLAIN;
     }
     if (k == FFR_KERNEL_PLAIN)
-        CU(c, c->L().occ(color, spill, &bps, &block, pb, nxf, &smem));
+        CU(c, c->L().occ(color, rsl_words_for(c->prog_host.data()), &bps, &block, pb, nxf,
+                         &smem));
     *kernel = k;
     if (bps < 1)
         return fail(c, FFR_ERR_ARG, "render kernel does not fit on an SM "
@@ -361,6 +362,7 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
     a.cancel = c->d_cancel;
     a.rng_words = program_words(c);
     a.agg = agg;
+    a.rsl_words = rsl_words_for(c->prog_host.data());
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
 }
 
@@ -1220,7 +1222,8 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
         {
             ffr_ctx* c = ctxs[m];
             size_t sm = 0;
-            if ((e = L.occ(g.color, 0, &bps, &block, (unsigned int)c->prog_host.size(),
+            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), &bps, &block,
+                           (unsigned int)c->prog_host.size(),
                            (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
                 return cfail(e, "occupancy");
             g.smem = std::max(g.smem, sm);

@@ -30,7 +30,7 @@ constexpr int kBlock = 128;
 template <bool C>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 {
-    const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf);
+    const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf, a.rsl_words);
     auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -41,9 +41,10 @@ static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 }
 
 template <bool C>
-static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, size_t* smem_out)
+static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_words,
+                           size_t* smem_out)
 {
-    const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf);
+    const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf, rsl_words);
     auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -58,13 +59,12 @@ cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t 
     return a.color_dims > 0 ? launch_one<true>(a, grid, st) : launch_one<false>(a, grid, st);
 }
 
-cudaError_t FFR_NAME(occupancy)(int color, int spill, int* blocks_per_sm, int* block,
+cudaError_t FFR_NAME(occupancy)(int color, int rsl_words, int* blocks_per_sm, int* block,
                                 unsigned int prog_bytes, int nxf, size_t* smem)
 {
-    (void)spill;
     *block = kBlock;
-    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, smem)
-                 : occ_one<false>(blocks_per_sm, prog_bytes, nxf, smem);
+    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, smem)
+                 : occ_one<false>(blocks_per_sm, prog_bytes, nxf, rsl_words, smem);
 }
 
 template <bool C>

@@ -37,10 +37,12 @@ struct Prog
     const XformT<R>* xf;
     const VarT<R>* var;
     const R* color;
+    uint32_t present;       // ProgHeader::tier_a_present
 
     __device__ __forceinline__ void bind(const unsigned char* base)
     {
         h = reinterpret_cast<const ProgHeader<R>*>(base);
+        present = h->tier_a_present;
         thresh = reinterpret_cast<const uint64_t*>(base + h->off_thresh);
         xf = reinterpret_cast<const XformT<R>*>(base + h->off_xf);
         var = reinterpret_cast<const VarT<R>*>(base + h->off_var);
@@ -95,7 +97,7 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     {
         const VarT<R>& var = pg.var[k];
         R o[D];
-        variation<D, R>(var, t, o, rng);
+        variation<D, R>(var, t, o, rng, pg.present);
         const R w = var.weight;
 #pragma unroll
         for (int i = 0; i < D; ++i)
@@ -200,7 +202,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     const ProgHeader<R>& h = *pg.h;
     const int nxf = a.nxf;
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
-    uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + (16 + kIsaacRslWords) * BLOCK);
+    const int rsl_words = a.rsl_words;
+    uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + (16 + rsl_words) * BLOCK);
     unsigned long long* xfc_shared = reinterpret_cast<unsigned long long*>(xfc_local);
     const bool local_xfc = nxf <= kLocalXfCounters;
     if (local_xfc)
@@ -215,15 +218,18 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
         __syncthreads();
     }
 
-    DevIsaac<BLOCK, kIsaacRslWords> rng;
+    DevIsaac<BLOCK, kIsaacRslMax> rng;
     rng.mem = ismem + threadIdx.x;
     rng.rsl = ismem + 16 * BLOCK + threadIdx.x;
     // words one sample step can draw: the choice, the chosen xform's
     // variations, the final xform's
     const unsigned int low = 1u + h.rng_words_max + (h.has_final ? pg.xf[nxf].rng_words : 0u);
     // refill ahead, warp-uniformly, once some lane could run dry this step
+    // (only with a carry area: when every xform draws the same number of
+    // words the lanes stay in phase and run dry together anyway)
     auto refill_ahead = [&]() __attribute__((always_inline)) {
-        if (__any_sync(__activemask(), rng.cnt < low) && rng.cnt <= kIsaacRslWords - 16)
+        if (rsl_words > 16 && __any_sync(__activemask(), rng.cnt < low)
+                && (int)rng.cnt <= rsl_words - 16)
             rng.refill();
     };
 
@@ -468,8 +474,19 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     }
 }
 
+// Resident CTAs of 128 threads the register budget must allow.  FP32: 6,
+// so that flames whose xforms draw equal numbers of words (16-word ISAAC
+// result arrays, about 37 KB of shared memory per CTA) run 6 CTAs per SM;
+// the FP32 body fits in 80 registers without spilling.  FP64: 4 (its body
+// needs about 120 registers; at 80 it spills).
+template <typename R>
+__host__ __device__ constexpr int render_min_blocks()
+{
+    return sizeof(R) == 4 ? 6 : 4;
+}
+
 template <int D, typename R, bool COLOR, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 4) chaos_kernel(const RenderArgs a)
+__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
@@ -485,7 +502,7 @@ __global__ void __launch_bounds__(BLOCK, 4) chaos_kernel(const RenderArgs a)
 // job's arguments are copied to shared memory and its program is reloaded
 // only when the CTA moves to another job.
 template <int D, typename R, bool COLOR, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 4) chaos_batch_kernel(const BatchArgs b)
+__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_kernel(const BatchArgs b)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(16) RenderArgs s_args;

@@ -357,6 +357,34 @@ std::vector<uint8_t> build_program(const HostFlame& f)
     if (words > 255)
         throw FlameError("an xform draws more than 255 random words per application");
     h.rng_words_max = words;
+    h.draws_vary = 0;
+    for (int k = 1; k < nxf; ++k)
+    {
+        uint32_t a = 0, b = 0;
+        for (const auto& v : all[0]->vars)
+            a += v.rng_words;
+        for (const auto& v : all[k]->vars)
+            b += v.rng_words;
+        if (a != b)
+            h.draws_vary = 1;
+    }
+    // variation types present (selectable and final xforms): bits in the
+    // order linear, sinusoidal, spherical, swirl, horseshoe, polar, julia,
+    // then bit 7 for any other type
+    static const int32_t kTierA[7] = {V_LINEAR, V_SINUSOIDAL, V_SPHERICAL, V_SWIRL,
+                                      V_HORSESHOE, V_POLAR, V_JULIA};
+    uint32_t present = 0;
+    for (const HostXform* x : all)
+        if (x)
+            for (const auto& v : x->vars)
+            {
+                uint32_t bit = 1u << 7;
+                for (int k = 0; k < 7; ++k)
+                    if (v.type == kTierA[k])
+                        bit = 1u << k;
+                present |= bit;
+            }
+    h.tier_a_present = present;
     for (int i = 0; i < f.dims; ++i)
     {
         h.size[i] = f.size[i];

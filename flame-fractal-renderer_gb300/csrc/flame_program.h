@@ -75,6 +75,14 @@ struct alignas(16) ProgHeader
     uint32_t off_color;
     uint32_t total_bytes;
     uint32_t rng_words_max; // upper bound of RNG words one xform step draws
+    // which of the seven benchmark variations the flame uses (kTierABit..,
+    // variations.cuh); bit 7 = some other variation.  Uniform per program,
+    // so kernels branch on it without divergence.
+    uint32_t tier_a_present;
+    // 1 when selectable xforms draw different numbers of RNG words per
+    // application (lanes of a warp then consume their ISAAC blocks out of
+    // phase and the render kernels keep a carry area for refill ahead)
+    uint32_t draws_vary;
     uint64_t size[kMaxDims];
     uint64_t mult_i[kMaxDims];
     uint64_t cells;

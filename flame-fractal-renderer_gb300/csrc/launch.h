@@ -2,6 +2,7 @@
 // units.  Plain structs shared by host and device code.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -50,25 +51,39 @@ struct RenderArgs
     const volatile unsigned int* cancel;   // host-mapped cancel flag, or null
     int rng_words;                  // largest RNG draw of one xform (sorted kernel)
     int agg;                        // warp-aggregate increments of equal cells
+    int rsl_words;                  // ISAAC result array words (16 or kIsaacRslMax)
     unsigned long long isaac_init[16];
 };
 
 constexpr int kLocalXfCounters = 16;
-// ISAAC result array per render thread: one block plus a full block of
-// words carried across a refill-ahead (isaac64.cuh)
-constexpr int kIsaacRslWords = 32;
+// ISAAC result array per render thread: one 16-word block, plus a second
+// 16 words carried across a refill ahead (isaac64.cuh) when the flame's
+// xforms draw different numbers of words (ProgHeader::draws_vary)
+constexpr int kIsaacRslMax = 32;
+
+// result-array words for a program blob (16 or kIsaacRslMax)
+inline int rsl_words_for(const void* prog)
+{
+    static_assert(offsetof(ProgHeader<double>, draws_vary)
+                  == offsetof(ProgHeader<float>, draws_vary), "program header layout");
+    uint32_t v = 0;
+    memcpy(&v, static_cast<const unsigned char*>(prog) + offsetof(ProgHeader<double>, draws_vary),
+           sizeof v);
+    return v ? kIsaacRslMax : 16;
+}
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
 
 // Dynamic shared memory of the plain and batch render kernels: the program,
-// ISAAC state (randmem [16][BLOCK], results [kIsaacRslWords][BLOCK]), and
+// ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), and
 // per-thread u32 xform counters when nxf <= kLocalXfCounters, else one u64
 // counter per xform for the CTA.
 template <int BLOCK>
-__host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf)
+__host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf,
+                                                   int rsl_words)
 {
     size_t s = align16u(prog_bytes);
-    s += (16 + kIsaacRslWords) * (size_t)BLOCK * sizeof(uint64_t);
+    s += (16 + (size_t)rsl_words) * (size_t)BLOCK * sizeof(uint64_t);
     if (nxf <= kLocalXfCounters)
         s += (size_t)nxf * BLOCK * sizeof(uint32_t);
     else
@@ -146,7 +161,7 @@ struct IsaacInit
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \
     cudaError_t launch_render_p##P##_d##D(const RenderArgs&, int grid,          \
                                           cudaStream_t);                        \
-    cudaError_t occupancy_p##P##_d##D(int color, int spill, int* blocks_per_sm, \
+    cudaError_t occupancy_p##P##_d##D(int color, int rsl_words, int* blocks_per_sm, \
                                       int* block, unsigned int prog_bytes,      \
                                       int nxf, size_t* smem);                   \
     cudaError_t launch_sorted_p##P##_d##D(const RenderArgs&, int grid,          \

@@ -177,7 +177,8 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     const int nxf = (int)f.xforms.size();
     int bps = 0, block = 0, sms = 1;
     size_t smem = 0;
-    if ((e = occ(f.color_dims > 0, 0, &bps, &block, (unsigned int)prog.size(), nxf, &smem))
+    if ((e = occ(f.color_dims > 0, rsl_words_for(prog.data()), &bps, &block,
+                 (unsigned int)prog.size(), nxf, &smem))
             != cudaSuccess)
         return nocuda(e, "occupancy");
     if (bps < 1)
@@ -232,6 +233,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     a.colors = d_colors;
     a.stats = dstats;
     a.cancel = nullptr;
+    a.rsl_words = rsl_words_for(prog.data());
     isaac_init_table(a.isaac_init);
     if ((e = render(a, (int)blocks, st)) != cudaSuccess)
         return nocuda(e, "render launch");

@@ -406,6 +406,7 @@ bool Server::launch_round_locked()
             a.cancel = d_cancel + j->slot;
             a.rng_words = b.rng_words;
             a.agg = 0;
+            a.rsl_words = rsl_words_for(b.prog.data());
             std::memcpy(a.isaac_init, isaac_init, sizeof a.isaac_init);
             jd.chunk_begin = groups[g].chunks;
             jd.chunks = take[i];
@@ -908,6 +909,7 @@ void ffr_server_destroy(ffr_server* srv)
             j->status = FFR_ERR_TIMEOUT;
         }
         s->queue.clear();
+        s->cv_done.notify_all();
         for (SrvJob* j : s->active)
         {
             j->cancel_req = true;
@@ -923,8 +925,14 @@ void ffr_server_destroy(ffr_server* srv)
 
 const char* ffr_server_last_error(const ffr_server* srv)
 {
-    const Server* s = reinterpret_cast<const Server*>(srv);
-    return s ? s->err.c_str() : g_server_error.c_str();
+    Server* s = reinterpret_cast<Server*>(const_cast<ffr_server*>(srv));
+    if (!s)
+        return g_server_error.c_str();
+    // a copy per calling thread: other threads may set the message meanwhile
+    thread_local std::string copy;
+    std::lock_guard<std::mutex> lk(s->mu);
+    copy = s->err;
+    return copy.c_str();
 }
 
 ffr_status ffr_server_submit(ffr_server* srv, const char* json, size_t len, const void* init,
@@ -960,7 +968,8 @@ ffr_status ffr_server_submit(ffr_server* srv, const char* json, size_t len, cons
         std::memcpy(b->init.data(), init, b->file_bytes());
     }
     b->smem = chaos_smem_bytes<kChunkStreams>((unsigned int)b->prog.size(),
-                                              (int)b->flame.xforms.size());
+                                              (int)b->flame.xforms.size(),
+                                              rsl_words_for(b->prog.data()));
     const uint64_t need = kStagingBytes + b->prog.size() + b->counts_bytes() + b->colors_bytes()
         + sizeof(DevStats) + (init ? b->file_bytes() : 0);
     if (need > s->budget)

@@ -214,77 +214,131 @@ __host__ __device__ inline bool tier_a(int type)
     return type >= 0 && type < 64 && ((kTierAMask >> type) & 1ull);
 }
 
-// The seven benchmark variations with their shared primitives merged.  In a
-// warp whose lanes apply different variations, the 98-way switch runs one
-// body per distinct type; here sqrt(r^2) is computed once for horseshoe,
-// polar and julia lanes, atan2 once for polar and julia lanes, and one
-// sincos serves swirl (of r^2) and julia (of the half angle), so a warp pays
-// each primitive at most once.  Every type still evaluates exactly the
-// expression of its case below, in the same operation order (the FP64
+// bits of ProgHeader::tier_a_present
+enum : uint32_t
+{
+    kTaLinear = 1u << 0, kTaSinusoidal = 1u << 1, kTaSpherical = 1u << 2, kTaSwirl = 1u << 3,
+    kTaHorseshoe = 1u << 4, kTaPolar = 1u << 5, kTaJulia = 1u << 6, kTaOther = 1u << 7
+};
+
+// The seven benchmark variations in one body.  In a warp whose lanes apply
+// different variations, the 98-way switch runs one body per distinct type,
+// each behind a divergent branch.  Here every shared primitive (sqrt of r^2
+// for horseshoe/polar/julia, atan2 for polar/julia, one sincos for swirl and
+// julia, one reciprocal for spherical and horseshoe) is computed by every
+// lane, once, guarded only by `present` (the flame's set of types, uniform
+// across the grid), and each lane selects its own result; the only per-lane
+// branch left is julia's random word.  Every type still evaluates exactly
+// its reference expression in the reference's operation order (the FP64
 // results are bit-identical to the switch), and julia draws its word at the
 // same point of the RNG sequence.
 template <int D, typename R, typename Rng>
-__device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R* out, Rng& rng)
+__device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R* out, Rng& rng,
+                                                 uint32_t present)
 {
     using T = RealTraits<R>;
     const int ty = v.type;
-    if (ty < kFirst2D)
+    const bool is_sin = ty == V_SINUSOIDAL, is_sph = ty == V_SPHERICAL;
+    if (!(present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
     {
-        if (ty == V_SINUSOIDAL)     /* 183-191 */
+        // only N-D types in the flame: no plane coordinates needed
+        R k = R(0);
+        if (present & kTaSpherical)
+            k = T::recip_(nsq<D>(t) + T::eps);          /* spherical 197-208 */
+#pragma unroll
+        for (int i = 0; i < D; ++i)
         {
-            for (int i = 0; i < D; ++i) out[i] = T::sin_(t[i]);
-        }
-        else if (ty == V_SPHERICAL) /* 197-208 */
-        {
-            const R r = T::recip_(nsq<D>(t) + T::eps);
-            for (int i = 0; i < D; ++i) out[i] = t[i] * r;
-        }
-        else                        /* 169-177 linear */
-        {
-            for (int i = 0; i < D; ++i) out[i] = t[i];
+            R o = t[i];                                 /* linear 169-177 */
+            if (present & kTaSinusoidal)                /* sinusoidal 183-191 */
+            {
+                const R sn = T::sin_(t[i]);
+                o = is_sin ? sn : o;
+            }
+            if (present & kTaSpherical)
+            {
+                const R sp = t[i] * k;
+                o = is_sph ? sp : o;
+            }
+            out[i] = o;
         }
         return;
     }
+    const bool is_nd = ty < kFirst2D;
+    const bool is_sw = ty == V_SWIRL, is_hs = ty == V_HORSESHOE, is_po = ty == V_POLAR,
+               is_ju = ty == V_JULIA;
     const int ax = v.axis_x, ay = v.axis_y;
     const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-    const R q = x * x + y * y;
-    const bool is_swirl = ty == V_SWIRL, is_julia = ty == V_JULIA;
-    R rt = R(0), ang = R(0), s = R(0), c = R(0);
-    if (!is_swirl)                  // horseshoe, polar, julia: sqrt(x^2 + y^2)
-        rt = T::sqrt_(q);
-    if (ty == V_POLAR || is_julia)  // atan2(y, x)
+    const R q = x * x + y * y;                          /* R2SQ */
+    R rt = R(0), ang = R(0), s = R(0), c = R(0), k = R(0);
+    if (present & (kTaHorseshoe | kTaPolar | kTaJulia))
+        rt = T::sqrt_(q);                               /* R2 */
+    if (present & (kTaPolar | kTaJulia))
         ang = T::atan2_(y, x);
-    if (is_swirl || is_julia)
+    if (present & (kTaSwirl | kTaJulia))
     {
-        R arg = q;                  /* swirl 509-522: sincos(r^2) */
-        if (is_julia)               /* julia 807-819: a/2 + pi * randBool */
-            arg = R(0.5) * ang + (R)(rng.next() & 1u) * T::pi;
+        R arg = q;                                      /* swirl 509-522: sincos(r^2) */
+        if (present & kTaJulia)
+        {
+            R bit = R(0);
+            if (is_ju)                                  /* julia 807-819: randBool */
+                bit = (R)(rng.next() & 1u);
+            const R ja = R(0.5) * ang + bit * T::pi;
+            arg = is_ju ? ja : arg;
+        }
         T::sincos_(arg, &s, &c);
     }
-    R X, Y;
-    if (is_swirl)
+    if (present & (kTaSpherical | kTaHorseshoe))
     {
-        X = x * s - y * c;
-        Y = x * c + y * s;
+        R den = rt + T::eps;                            /* horseshoe 527-540 */
+        if (present & kTaSpherical)
+        {
+            const R ds = nsq<D>(t) + T::eps;            /* spherical 197-208 */
+            den = is_sph ? ds : den;
+        }
+        k = T::recip_(den);
     }
-    else if (ty == V_HORSESHOE)     /* 527-540 */
+    R X = R(0), Y = R(0);
+    if (present & kTaSwirl)
     {
-        const R r = T::recip_(rt + T::eps);
-        X = ((x - y) * (x + y)) * r;
-        Y = (R(2.0) * x * y) * r;
+        const R a0 = x * s - y * c, a1 = x * c + y * s;
+        X = is_sw ? a0 : X;
+        Y = is_sw ? a1 : Y;
     }
-    else if (ty == V_POLAR)         /* 545-555 */
+    if (present & kTaHorseshoe)
     {
-        X = ang * T::inv_pi;
-        Y = rt - R(1.0);
+        const R a0 = ((x - y) * (x + y)) * k, a1 = (R(2.0) * x * y) * k;
+        X = is_hs ? a0 : X;
+        Y = is_hs ? a1 : Y;
     }
-    else                            /* julia */
+    if (present & kTaPolar)                             /* polar 545-555 */
     {
-        X = c * rt;
-        Y = s * rt;
+        const R a0 = ang * T::inv_pi, a1 = rt - R(1.0);
+        X = is_po ? a0 : X;
+        Y = is_po ? a1 : Y;
     }
+    if (present & kTaJulia)
+    {
+        const R a0 = c * rt, a1 = s * rt;
+        X = is_ju ? a0 : X;
+        Y = is_ju ? a1 : Y;
+    }
+#pragma unroll
     for (int i = 0; i < D; ++i)
-        out[i] = i == ax ? X : (i == ay ? Y : R(0));
+    {
+        R o = t[i];                                     /* linear 169-177 */
+        if (present & kTaSinusoidal)                    /* sinusoidal 183-191 */
+        {
+            const R sn = T::sin_(t[i]);
+            o = is_sin ? sn : o;
+        }
+        if (present & kTaSpherical)
+        {
+            const R sp = t[i] * k;
+            o = is_sph ? sp : o;
+        }
+        const R p2 = i == ax ? X : (i == ay ? Y : R(0));
+        out[i] = is_nd ? o : p2;
+    }
 }
 
 // one variation: o = V(t).  Restates each class of
@@ -294,12 +348,13 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
 // through rng.next() in the reference's order (FlameRNG,
 // src/rng/flame_rng.hpp).
 template <int D, typename R, typename Rng>
-__device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng)
+__device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng,
+                                          uint32_t present = ~0u)
 {
     using T = RealTraits<R>;
     if (tier_a(v.type))
     {
-        variation_tier_a<D, R>(v, t, o, rng);
+        variation_tier_a<D, R>(v, t, o, rng, present);
         return;
     }
     const int ax = v.axis_x, ay = v.axis_y;

@@ -48,6 +48,7 @@ EXPORTS = [
     "ffr_render_image", "ffr_encode_png",
 ]
 IMG_CLI_PATH = os.path.join(HERE, "_build", "ffr-img")
+SERVE_CLI_PATH = os.path.join(HERE, "_build", "ffr-serve")
 IMAGE_MONO, IMAGE_GRAY, IMAGE_RGB = 0, 1, 2
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
@@ -582,3 +583,97 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---------------------------------------------------------------- wire client
+# Framing of include/ffr_wire.h (little-endian, packed).
+WIRE_VERSION = 1
+WIRE_SUBMIT, WIRE_CONTINUE, WIRE_WAIT, WIRE_READ, WIRE_POLL, WIRE_CANCEL, WIRE_RELEASE, \
+    WIRE_SHUTDOWN = range(1, 9)
+WIRE_WITH_BUFFER = 1
+_REQ = "<4sIII7Q"           # 72 bytes
+_RSP = "<4sIQII7Q"          # 80 bytes
+
+
+def pack_request(op: int, job: int = 0, samples: int = 0, seed: int = 0, bad_limit: int = 256,
+                 timeout_ms: int = 0, flags: int = 0, json_text: bytes = b"",
+                 init: bytes = b"") -> bytes:
+    import struct
+    return struct.pack(_REQ, b"FFRQ", WIRE_VERSION, op, flags, job, samples, seed, bad_limit,
+                       timeout_ms, len(json_text), len(init)) + json_text + init
+
+
+def unpack_response(head: bytes) -> dict:
+    import struct
+    (magic, status, job, state, job_status, samples, buffer_bytes, parent, submit_ns, admit_ns,
+     done_ns, payload_len) = struct.unpack(_RSP, head)
+    if magic != b"FFRR":
+        raise FfrError(FFR_ERR_IO, "bad response frame")
+    return {"status": status, "job": job, "state": state, "job_status": job_status,
+            "samples": samples, "buffer_bytes": buffer_bytes, "parent": parent,
+            "submit_ns": submit_ns, "admit_ns": admit_ns, "done_ns": done_ns,
+            "payload_len": payload_len}
+
+
+class RemoteServer:
+    """Client of ffr-serve over a socket (or any pair of binary streams)."""
+
+    def __init__(self, host: str = "127.0.0.1", port: int = 0, rfile=None, wfile=None):
+        import socket
+        if rfile is None:
+            self._sock = socket.create_connection((host, port))
+            self._r = self._sock.makefile("rb")
+            self._w = self._sock.makefile("wb")
+        else:
+            self._sock, self._r, self._w = None, rfile, wfile
+
+    def _call(self, frame: bytes):
+        import struct
+        self._w.write(frame)
+        self._w.flush()
+        head = self._r.read(struct.calcsize(_RSP))
+        if len(head) != struct.calcsize(_RSP):
+            raise FfrError(FFR_ERR_IO, "connection closed")
+        rsp = unpack_response(head)
+        payload = self._r.read(rsp["payload_len"]) if rsp["payload_len"] else b""
+        if rsp["status"] not in (FFR_OK, FFR_BAD_VALUES):
+            raise FfrError(rsp["status"], payload.decode("utf-8", "replace"))
+        return rsp, payload
+
+    def submit(self, flame, samples: int, seed: int, bad_limit: int = 256, init: bytes = b""):
+        text = flame if isinstance(flame, str) else json.dumps(flame)
+        return self._call(pack_request(WIRE_SUBMIT, samples=samples, seed=seed,
+                                       bad_limit=bad_limit, json_text=text.encode(),
+                                       init=init))[0]["job"]
+
+    def continue_(self, parent: int, samples: int, seed: int, bad_limit: int = 256):
+        return self._call(pack_request(WIRE_CONTINUE, job=parent, samples=samples, seed=seed,
+                                       bad_limit=bad_limit))[0]["job"]
+
+    def wait(self, job: int, timeout_ms: int = 0, with_buffer: bool = False):
+        return self._call(pack_request(WIRE_WAIT, job=job, timeout_ms=timeout_ms,
+                                       flags=WIRE_WITH_BUFFER if with_buffer else 0))
+
+    def read(self, job: int) -> bytes:
+        return self._call(pack_request(WIRE_READ, job=job))[1]
+
+    def poll(self, job: int) -> dict:
+        return self._call(pack_request(WIRE_POLL, job=job))[0]
+
+    def cancel(self, job: int) -> None:
+        self._call(pack_request(WIRE_CANCEL, job=job))
+
+    def release(self, job: int) -> None:
+        self._call(pack_request(WIRE_RELEASE, job=job))
+
+    def shutdown(self) -> None:
+        self._call(pack_request(WIRE_SHUTDOWN))
+
+    def close(self):
+        for f in (self._r, self._w):
+            try:
+                f.close()
+            except Exception:
+                pass
+        if self._sock is not None:
+            self._sock.close()
