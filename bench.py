@@ -305,9 +305,10 @@ def run_sierpinski(args):
     res = {}
     sampler = ClockSampler(dev)
     sampler.start()
+    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED}
     for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
         with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
-                                device=dev) as r:
+                                device=dev, kernel=kern[args.kernel]) as r:
             ms, binned, iters, s = _timed_steps(r, args, N, 1, flush)
             res[name] = {"value": binned / (ms * 1e-3), "ms_per_step": ms / args.steps,
                          "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel)}
@@ -496,6 +497,9 @@ def run_serving(args):
     results = []
 
     def completer():
+        # one host buffer per client thread, grown as needed and reused (a
+        # client that writes results out does not fault in fresh pages per read)
+        out = np.empty(0, dtype=np.uint64)
         while True:
             j = done.get()
             if j is None:
@@ -505,8 +509,9 @@ def run_serving(args):
                 kind, cells, dims = info[j]
                 st = srv.stats(j, dims)
                 t0 = time.perf_counter_ns()
-                out = np.empty(cells, dtype=np.uint64)
-                srv.read_into(j, out.ctypes.data, out.nbytes)
+                if out.size < cells:
+                    out = np.ones(cells, dtype=np.uint64)
+                srv.read_into(j, out.ctypes.data, cells * 8)
                 t_read = time.perf_counter_ns() - t0
             except Exception as e:          # noqa: BLE001
                 errors.append(repr(e))

@@ -47,7 +47,8 @@ namespace {
 constexpr int kChunkStreams = 128;          // BLOCK of the batch kernel
 constexpr int kRoundSlots = 2;
 constexpr int kGroups = 6;                  // dims 1..3 x colour off/on
-constexpr size_t kStagingBytes = 16u << 20; // read staging, file layout
+constexpr size_t kStagingBytes = 16u << 20; // device staging of one read slot
+constexpr int kReadSlots = 4;               // concurrent buffer reads
 
 uint64_t now_ns()
 {
@@ -130,7 +131,22 @@ struct Server
     unsigned long long isaac_init[16] = {};
     cudaMemPool_t pool = nullptr;
     cudaStream_t aux = nullptr;         // allocations, resets, statistics
-    cudaStream_t io = nullptr;          // buffer reads
+    // Buffer reads.  Each slot exports a slice of cells into its device
+    // staging, copies it into one of two pinned host buffers (a true async
+    // DMA: a copy into the caller's pageable memory would be a synchronous
+    // driver call that holds up the scheduler's launches) and the host then
+    // copies the previous slice out while the next one is in flight.
+    struct ReadSlot
+    {
+        cudaStream_t stream = nullptr;
+        unsigned long long* d_stage = nullptr;
+        unsigned char* h_stage[2] = {nullptr, nullptr};
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        bool busy = false;
+    };
+    ReadSlot readers[kReadSlots];
+    std::mutex rd_mu;
+    std::condition_variable rd_cv;
     cudaEvent_t ev_alloc = nullptr;     // after the latest admission work
     unsigned int* h_cancel = nullptr;   // mapped pinned flags, one per slot
     unsigned int* d_cancel = nullptr;
@@ -151,8 +167,6 @@ struct Server
     std::thread thread;
 
     std::atomic<uint64_t> used{0}, peak{0};
-    std::mutex io_mu;
-    unsigned long long* d_staging = nullptr;    // kStagingBytes
 
     void add_used(size_t b)
     {
@@ -701,11 +715,21 @@ void server_free(Server* s)
         if (r.stream)
             cudaStreamDestroy(r.stream);
     }
-    cudaFree(s->d_staging);
-    if (s->io)
+    for (auto& r : s->readers)
     {
-        cudaStreamSynchronize(s->io);
-        cudaStreamDestroy(s->io);
+        if (r.stream)
+        {
+            cudaStreamSynchronize(r.stream);
+            cudaStreamDestroy(r.stream);
+        }
+        cudaFree(r.d_stage);
+        for (int k = 0; k < 2; ++k)
+        {
+            if (r.h_stage[k])
+                cudaFreeHost(r.h_stage[k]);
+            if (r.ev[k])
+                cudaEventDestroy(r.ev[k]);
+        }
     }
     if (s->aux)
     {
@@ -844,7 +868,7 @@ ffr_status ffr_server_create(const ffr_server_opts* opts, ffr_server** out)
     if ((e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
         return cfail(e, "cudaMemPoolSetAttribute");
     if ((e = cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking)) != cudaSuccess
-            || (e = cudaStreamCreateWithFlags(&s->io, cudaStreamNonBlocking)) != cudaSuccess)
+            )
         return cfail(e, "cudaStreamCreate");
     if ((e = cudaEventCreateWithFlags(&s->ev_alloc, cudaEventDisableTiming)) != cudaSuccess)
         return cfail(e, "cudaEventCreate");
@@ -877,11 +901,23 @@ ffr_status ffr_server_create(const ffr_server_opts* opts, ffr_server** out)
     const uint64_t reserve = 2ull << 30;
     const uint64_t avail = fr > reserve ? fr - reserve : 0;
     s->budget = o.hbm_budget ? std::min<uint64_t>(o.hbm_budget, avail) : avail;
-    if (s->budget < kStagingBytes)
+    if (s->budget < kStagingBytes * kReadSlots)
         return cfail(cudaErrorMemoryAllocation, "device-memory budget below the read staging");
-    if ((e = cudaMalloc(&s->d_staging, kStagingBytes)) != cudaSuccess)
-        return cfail(e, "cudaMalloc(read staging)");
-    s->add_used(kStagingBytes);
+    for (auto& r : s->readers)
+    {
+        if ((e = cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return cfail(e, "cudaStreamCreate");
+        if ((e = cudaMalloc(&r.d_stage, kStagingBytes)) != cudaSuccess)
+            return cfail(e, "cudaMalloc(read staging)");
+        for (int k = 0; k < 2; ++k)
+        {
+            if ((e = cudaHostAlloc(&r.h_stage[k], kStagingBytes, 0)) != cudaSuccess)
+                return cfail(e, "cudaHostAlloc(read staging)");
+            if ((e = cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming)) != cudaSuccess)
+                return cfail(e, "cudaEventCreate");
+        }
+        s->add_used(kStagingBytes);
+    }
     try
     {
         s->thread = std::thread([s] { s->loop(); });
@@ -970,7 +1006,8 @@ ffr_status ffr_server_submit(ffr_server* srv, const char* json, size_t len, cons
     b->smem = chaos_smem_bytes<kChunkStreams>((unsigned int)b->prog.size(),
                                               (int)b->flame.xforms.size(),
                                               rsl_words_for(b->prog.data()));
-    const uint64_t need = kStagingBytes + b->prog.size() + b->counts_bytes() + b->colors_bytes()
+    const uint64_t need = kStagingBytes * kReadSlots + b->prog.size() + b->counts_bytes()
+        + b->colors_bytes()
         + sizeof(DevStats) + (init ? b->file_bytes() : 0);
     if (need > s->budget)
         return sfail(s, FFR_ERR_OOM, "buffer needs " + std::to_string(need)
@@ -1132,26 +1169,65 @@ ffr_status ffr_server_read(ffr_server* srv, uint64_t job, void* cells, size_t by
     const size_t need = b->file_bytes();
     if (!cells || bytes < need)
         return sfail(s, FFR_ERR_IO, "error writing output: destination too small");
-    // export through the fixed staging area, a slice of cells at a time
-    std::lock_guard<std::mutex> io(s->io_mu);
+    // a free read slot
+    Server::ReadSlot* r = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(s->rd_mu);
+        for (;;)
+        {
+            for (auto& x : s->readers)
+                if (!x.busy)
+                {
+                    r = &x;
+                    break;
+                }
+            if (r)
+                break;
+            s->rd_cv.wait(lk);
+        }
+        r->busy = true;
+    }
     cudaSetDevice(s->o.device);
     const size_t words = 1 + (size_t)b->flame.color_dims;
     const uint64_t step = std::max<uint64_t>(1, kStagingBytes / 8 / words);
-    cudaError_t e = cudaStreamWaitEvent(s->io, s->ev_alloc, 0);
-    for (uint64_t c0 = 0; c0 < b->flame.cells && e == cudaSuccess; c0 += step)
+    const uint64_t nslices = (b->flame.cells + step - 1) / step;
+    unsigned char* dst = static_cast<unsigned char*>(cells);
+    auto slice_cells = [&](uint64_t k) { return std::min<uint64_t>(step, b->flame.cells - k * step); };
+    cudaError_t e = cudaStreamWaitEvent(r->stream, s->ev_alloc, 0);
+    for (uint64_t k = 0; k <= nslices && e == cudaSuccess; ++k)
     {
-        const uint64_t n = std::min<uint64_t>(step, b->flame.cells - c0);
-        e = launch_export(s->d_staging, n, b->flame.color_dims, b->d_counts + c0,
-                          b->d_hi ? b->d_hi + c0 : nullptr,
-                          b->d_colors ? b->d_colors + c0 * b->flame.color_dims : nullptr, s->io);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(static_cast<unsigned char*>(cells) + c0 * words * 8, s->d_staging,
-                                n * words * 8, cudaMemcpyDeviceToHost, s->io);
-        // the staging area is reused by the next slice: stream order keeps
-        // the export behind the previous copy
+        if (k < nslices)
+        {
+            // slice k: export, DMA into pinned buffer k % 2 (its previous
+            // slice, k - 2, was copied out in the previous iteration)
+            const uint64_t c0 = k * step, n = slice_cells(k);
+            e = launch_export(r->d_stage, n, b->flame.color_dims, b->d_counts + c0,
+                              b->d_hi ? b->d_hi + c0 : nullptr,
+                              b->d_colors ? b->d_colors + c0 * b->flame.color_dims : nullptr,
+                              r->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(r->h_stage[k & 1], r->d_stage, n * words * 8,
+                                    cudaMemcpyDeviceToHost, r->stream);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(r->ev[k & 1], r->stream);
+        }
+        if (k >= 1 && e == cudaSuccess)
+        {
+            // slice k - 1 to the caller while slice k is in flight
+            const uint64_t j = k - 1;
+            e = cudaEventSynchronize(r->ev[j & 1]);
+            if (e == cudaSuccess)
+                std::memcpy(dst + j * step * words * 8, r->h_stage[j & 1],
+                            slice_cells(j) * words * 8);
+        }
     }
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(s->io);
+    if (e != cudaSuccess)
+        cudaStreamSynchronize(r->stream);
+    {
+        std::lock_guard<std::mutex> lk(s->rd_mu);
+        r->busy = false;
+    }
+    s->rd_cv.notify_one();
     if (e != cudaSuccess)
         return sfail(s, FFR_ERR_CUDA, std::string("read: ") + cudaGetErrorString(e));
     return FFR_OK;

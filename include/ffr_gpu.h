@@ -259,7 +259,7 @@ typedef struct ffr_server_opts {
     uint64_t settle;           /* default 53 */
     uint64_t traj_len;         /* samples per stream; default 4096 */
     /* device bytes the server may hold: buffers, per-job statistics
-       (about 170 KB each) and a fixed 16 MiB read staging area;
+       (about 170 KB each) and a fixed 64 MiB of read staging (4 slots);
        0 = free device memory at creation minus 2 GiB */
     uint64_t hbm_budget;
     uint64_t max_active;       /* jobs admitted at once; default 256 */

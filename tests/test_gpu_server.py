@@ -145,13 +145,13 @@ def test_init_buffer_is_added(ffr, flames):
 
 
 def test_admission_respects_memory_budget(ffr, flames):
-    """With a budget that holds two 1024x1024 buffers (besides the 16 MiB
+    """With a budget that holds two 1024x1024 buffers (besides the 64 MiB
     read staging), the third job waits in the queue until a finished job's
     buffer is released; the device bytes held never pass the budget and every
     result is still exact."""
     side = 1024
     per = side * side * 4 + 200_000
-    budget = (16 << 20) + int(2.5 * per)
+    budget = (64 << 20) + int(2.5 * per)
     texts = [json.dumps(flames.random_2d(40 + i, size=(side, side))) for i in range(4)]
     with ffr.Server(precision=1, settle=SETTLE, hbm_budget=budget) as srv:
         ids = [srv.submit(t, 1_500_000, 60 + i) for i, t in enumerate(texts)]
@@ -173,9 +173,9 @@ def test_admission_respects_memory_budget(ffr, flames):
 
 
 def test_too_large_for_budget_is_rejected(ffr, flames):
-    """A buffer larger than the whole budget (16 MiB staging + 1 MiB here) is
+    """A buffer larger than the whole budget (64 MiB staging + 1 MiB here) is
     refused at submission instead of waiting forever."""
-    with ffr.Server(precision=1, settle=SETTLE, hbm_budget=(16 << 20) + (1 << 20)) as srv:
+    with ffr.Server(precision=1, settle=SETTLE, hbm_budget=(64 << 20) + (1 << 20)) as srv:
         with pytest.raises(ffr.FfrError) as e:
             srv.submit(json.dumps(flames.random_2d(1, size=(1024, 1024))), 10, 1)
         assert e.value.status == ffr.FFR_ERR_OOM
@@ -249,3 +249,26 @@ def test_budget_below_staging_is_refused(ffr):
     with pytest.raises(ffr.FfrError) as e:
         ffr.Server(precision=1, hbm_budget=1 << 20)
     assert e.value.status == ffr.FFR_ERR_CUDA
+
+
+def test_concurrent_and_multi_slice_reads(ffr, flames):
+    """Reads from several threads at once (the server has four read slots)
+    and reads larger than one 16 MiB staging slice return the exact buffers."""
+    import concurrent.futures as cf
+    big = json.dumps(flames.random_3d(5, size=(200, 200, 200)))      # 64 MB file: 4 slices
+    col = golden_flame_text("color")                                  # colour channels
+    small = [json.dumps(flames.random_2d(300 + i, size=(256, 144))) for i in range(6)]
+    jobs = [(big, 3_000_000, 1, 200 ** 3, 0), (col, 400_000, 2, 80 * 60, 3)]
+    jobs += [(t, 500_000, 10 + i, 256 * 144, 0) for i, t in enumerate(small)]
+    with ffr.Server(precision=1, settle=SETTLE) as srv:
+        ids = [srv.submit(t, n, seed) for t, n, seed, _, _ in jobs]
+        for j in ids:
+            assert srv.wait(j, 120_000).state == ffr.JOB_DONE
+        with cf.ThreadPoolExecutor(8) as ex:
+            got = list(ex.map(lambda a: srv.read(a[0], a[1][3], a[1][4]), zip(ids, jobs)))
+    for (t, n, seed, cells, r), g in zip(jobs, got):
+        want, _, _ = solo(ffr, t, n, seed, 1)
+        np.testing.assert_array_equal(g[:, 0], want[:, 0])
+        if r:
+            np.testing.assert_allclose(g[:, 1:].copy().view(np.float64),
+                                       want[:, 1:].copy().view(np.float64), rtol=1e-12, atol=1e-9)
