@@ -364,6 +364,7 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
     a.agg = agg;
     a.rsl_words = rsl_words_for(c->prog_host.data());
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
+    set_geometry(a, c->prog_host.data(), c->opts.precision);
 }
 
 // the leading fields of DevStats (everything before xf_dist)

@@ -92,12 +92,28 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
 #pragma unroll
     for (int i = 0; i < D; ++i)
         v[i] = R(0);
+    // 2-D flames: the plane primitives of the benchmark variations, once
+    // per application (the same values every variation would compute)
+    PlanePrims<R> pp;
+    pp.valid = false;
+    pp.q = pp.rt = pp.ang = R(0);
+    if (D == 2 && (pg.present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+    {
+        using T = RealTraits<R>;
+        const R px = t[0], py = t[D - 1];
+        pp.valid = true;
+        pp.q = px * px + py * py;
+        if (pg.present & (kTaHorseshoe | kTaPolar | kTaJulia))
+            pp.rt = T::sqrt_(pp.q);
+        if (pg.present & (kTaPolar | kTaJulia))
+            pp.ang = T::atan2_(py, px);
+    }
     const int vb = x.var_begin, ve = x.var_begin + x.var_count;
     for (int k = vb; k < ve; ++k)
     {
         const VarT<R>& var = pg.var[k];
         R o[D];
-        variation<D, R>(var, t, o, rng, pg.present);
+        variation<D, R>(var, t, o, rng, pg.present, pp);
         const R w = var.weight;
 #pragma unroll
         for (int i = 0; i < D; ++i)
@@ -152,6 +168,34 @@ template <> __device__ __forceinline__ uint64_t to_index<float>(float x)
 {
     return (uint64_t)x;
 }
+
+// The same truncation to 32 bits.  An in-bounds coordinate gives a value in
+// [0, size] with size <= 65535 (Flame validation), where the 32-bit and the
+// 64-bit conversions agree.
+template <typename R> __device__ __forceinline__ uint32_t to_index32(R x);
+template <> __device__ __forceinline__ uint32_t to_index32<double>(double x)
+{
+    return (uint32_t)x;
+}
+template <> __device__ __forceinline__ uint32_t to_index32<float>(float x)
+{
+    return (uint32_t)x;
+}
+
+// geometry of RenderArgs in the kernel's precision
+template <typename R> struct Geo;
+template <> struct Geo<double>
+{
+    __device__ static __forceinline__ double lo(const RenderArgs& a, int i) { return a.lo_d[i]; }
+    __device__ static __forceinline__ double hi(const RenderArgs& a, int i) { return a.hi_d[i]; }
+    __device__ static __forceinline__ double mult(const RenderArgs& a, int i) { return a.mult_d_d[i]; }
+};
+template <> struct Geo<float>
+{
+    __device__ static __forceinline__ float lo(const RenderArgs& a, int i) { return a.lo_f[i]; }
+    __device__ static __forceinline__ float hi(const RenderArgs& a, int i) { return a.hi_f[i]; }
+    __device__ static __forceinline__ float mult(const RenderArgs& a, int i) { return a.mult_d_f[i]; }
+};
 
 template <typename R>
 __device__ __forceinline__ double as_double(R x) { return (double)x; }
@@ -233,7 +277,13 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
             rng.refill();
     };
 
-    unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
+    // per-thread counters fit 32 bits: a thread runs fewer than 2^32
+    // samples (checked by the launch planners)
+    unsigned int s_iter = 0, s_plot = 0, dropped = 0;
+    using G = Geo<R>;
+    // below 2^30 cells the index sum (per-axis indices can reach the axis
+    // size in FP64, as in the reference) stays under 2^32
+    const bool idx32 = a.cells < (1ull << 30);
     R ext_lo[D], ext_hi[D];
 #pragma unroll
     for (int i = 0; i < D; ++i)
@@ -256,9 +306,10 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
         rng.seed(stream_key(a.seed, s), a.isaac_init);
         for (unsigned long long tj = s; tj < ntraj && !stop; tj += a.streams)
         {
-            unsigned long long len = a.samples - tj * L;
-            if (len > L)
-                len = L;
+            unsigned long long len64 = a.samples - tj * L;
+            if (len64 > L)
+                len64 = L;
+            unsigned int len = (unsigned int)len64;
             // _render_batch entry check (buffer_renderer.hpp:153)
             if (*vstop)
             {
@@ -370,32 +421,46 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 bool inb = true;
 #pragma unroll
                 for (int i = 0; i < D; ++i)
-                    inb &= (pf[i] >= h.lo[i]) && (pf[i] <= h.hi[i]);
+                    inb &= (pf[i] >= G::lo(a, i)) && (pf[i] <= G::hi(a, i));
                 if (inb)
                 {
                     ++s_plot;
                     uint64_t bi;
-                    if (sizeof(R) == sizeof(double))
+                    if (idx32)
+                    {
+                        // fewer than 2^30 cells: the index sum fits 32 bits
+                        uint32_t b = 0;
+#pragma unroll
+                        for (int i = 0; i < D; ++i)
+                        {
+                            uint32_t di = to_index32<R>((pf[i] - G::lo(a, i)) * G::mult(a, i));
+                            // FP32: per-axis index clamped to the axis
+                            if (sizeof(R) == sizeof(float))
+                                di = di < a.size32[i] ? di : a.size32[i] - 1u;
+                            b += di * (uint32_t)a.mult_i[i];
+                        }
+                        bi = b;
+                    }
+                    else if (sizeof(R) == sizeof(double))
                     {
                         // buffer_renderer.hpp:200-209
-                        bi = to_index<R>((pf[0] - h.lo[0]) * h.mult_d[0]);
+                        bi = to_index<R>((pf[0] - G::lo(a, 0)) * G::mult(a, 0));
 #pragma unroll
                         for (int i = 1; i < D; ++i)
-                            bi += to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]) * h.mult_i[i];
+                            bi += to_index<R>((pf[i] - G::lo(a, i)) * G::mult(a, i)) * a.mult_i[i];
                     }
                     else
                     {
-                        // FP32: per-axis index clamped to the axis
                         bi = 0;
 #pragma unroll
                         for (int i = 0; i < D; ++i)
                         {
-                            uint64_t di = to_index<R>((pf[i] - h.lo[i]) * h.mult_d[i]);
-                            di = di < h.size[i] ? di : h.size[i] - 1;
-                            bi += di * h.mult_i[i];
+                            uint64_t di = to_index<R>((pf[i] - G::lo(a, i)) * G::mult(a, i));
+                            di = di < a.size32[i] ? di : a.size32[i] - 1u;
+                            bi += di * a.mult_i[i];
                         }
                     }
-                    if (bi < h.cells)
+                    if (bi < a.cells)
                     {
                         bin_count(a, bi);
                         if (COLOR)
@@ -419,14 +484,15 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
         }
     }
 
-    // merge statistics: warp reduce, then one atomic per warp
+    // merge statistics: warp reduce (in 64 bits), then one atomic per warp
     const unsigned int lane = threadIdx.x & 31u;
+    unsigned long long w_iter = s_iter, w_plot = s_plot, w_dropped = dropped;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
     {
-        s_iter += __shfl_down_sync(0xffffffffu, s_iter, off);
-        s_plot += __shfl_down_sync(0xffffffffu, s_plot, off);
-        dropped += __shfl_down_sync(0xffffffffu, dropped, off);
+        w_iter += __shfl_down_sync(0xffffffffu, w_iter, off);
+        w_plot += __shfl_down_sync(0xffffffffu, w_plot, off);
+        w_dropped += __shfl_down_sync(0xffffffffu, w_dropped, off);
 #pragma unroll
         for (int i = 0; i < D; ++i)
         {
@@ -438,12 +504,12 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     }
     if (lane == 0)
     {
-        if (s_iter)
-            atomicAdd(&a.stats->s_iter, s_iter);
-        if (s_plot)
-            atomicAdd(&a.stats->s_plot, s_plot);
-        if (dropped)
-            atomicAdd(&a.stats->dropped, dropped);
+        if (w_iter)
+            atomicAdd(&a.stats->s_iter, w_iter);
+        if (w_plot)
+            atomicAdd(&a.stats->s_plot, w_plot);
+        if (w_dropped)
+            atomicAdd(&a.stats->dropped, w_dropped);
 #pragma unroll
         for (int i = 0; i < D; ++i)
         {

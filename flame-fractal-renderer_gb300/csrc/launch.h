@@ -53,7 +53,48 @@ struct RenderArgs
     int agg;                        // warp-aggregate increments of equal cells
     int rsl_words;                  // ISAAC result array words (16 or kIsaacRslMax)
     unsigned long long isaac_init[16];
+    // the program header's geometry, copied here so the render loop reads
+    // it from kernel parameters instead of shared memory each sample
+    // (set_geometry); the bounds and scales in the kernel's precision
+    double lo_d[kMaxDims], hi_d[kMaxDims], mult_d_d[kMaxDims];
+    float lo_f[kMaxDims], hi_f[kMaxDims], mult_d_f[kMaxDims];
+    unsigned int size32[kMaxDims];          // buffer size per axis
+    unsigned long long mult_i[kMaxDims];    // cell stride per axis
+    unsigned long long cells;
 };
+
+// copy the geometry of a program blob (precision 0 FP64, 1 FP32) into a
+inline void set_geometry(RenderArgs& a, const void* prog, int precision)
+{
+    if (precision == 0)
+    {
+        ProgHeader<double> h;
+        memcpy(&h, prog, sizeof h);
+        for (int i = 0; i < kMaxDims; ++i)
+        {
+            a.lo_d[i] = h.lo[i];
+            a.hi_d[i] = h.hi[i];
+            a.mult_d_d[i] = h.mult_d[i];
+            a.size32[i] = (unsigned int)h.size[i];
+            a.mult_i[i] = h.mult_i[i];
+        }
+        a.cells = h.cells;
+    }
+    else
+    {
+        ProgHeader<float> h;
+        memcpy(&h, prog, sizeof h);
+        for (int i = 0; i < kMaxDims; ++i)
+        {
+            a.lo_f[i] = h.lo[i];
+            a.hi_f[i] = h.hi[i];
+            a.mult_d_f[i] = h.mult_d[i];
+            a.size32[i] = (unsigned int)h.size[i];
+            a.mult_i[i] = h.mult_i[i];
+        }
+        a.cells = h.cells;
+    }
+}
 
 constexpr int kLocalXfCounters = 16;
 // ISAAC result array per render thread: one 16-word block, plus a second

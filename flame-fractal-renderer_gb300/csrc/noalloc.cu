@@ -235,6 +235,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     a.cancel = nullptr;
     a.rsl_words = rsl_words_for(prog.data());
     isaac_init_table(a.isaac_init);
+    set_geometry(a, prog.data(), o.precision);
     if ((e = render(a, (int)blocks, st)) != cudaSuccess)
         return nocuda(e, "render launch");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess)

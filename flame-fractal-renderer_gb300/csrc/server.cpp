@@ -422,6 +422,7 @@ bool Server::launch_round_locked()
             a.agg = 0;
             a.rsl_words = rsl_words_for(b.prog.data());
             std::memcpy(a.isaac_init, isaac_init, sizeof a.isaac_init);
+            set_geometry(a, b.prog.data(), o.precision);
             jd.chunk_begin = groups[g].chunks;
             jd.chunks = take[i];
             jd.chunk_first = j->chunks_issued;

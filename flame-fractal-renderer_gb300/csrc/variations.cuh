@@ -221,6 +221,17 @@ enum : uint32_t
     kTaHorseshoe = 1u << 4, kTaPolar = 1u << 5, kTaJulia = 1u << 6, kTaOther = 1u << 7
 };
 
+// Primitives of the pre-affine point shared by the 2-D benchmark variations
+// of one xform application.  In a 2-D flame every 2-D variation acts on the
+// plane (0, 1), so they are computed once per application, not once per
+// variation (valid = false: the variation computes its own).
+template <typename R>
+struct PlanePrims
+{
+    bool valid;
+    R q, rt, ang;       // x^2 + y^2, sqrt of it, atan2(y, x)
+};
+
 // The seven benchmark variations in one body.  In a warp whose lanes apply
 // different variations, the 98-way switch runs one body per distinct type,
 // each behind a divergent branch.  Here every shared primitive (sqrt of r^2
@@ -234,7 +245,7 @@ enum : uint32_t
 // same point of the RNG sequence.
 template <int D, typename R, typename Rng>
 __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R* out, Rng& rng,
-                                                 uint32_t present)
+                                                 uint32_t present, const PlanePrims<R>& pp)
 {
     using T = RealTraits<R>;
     const int ty = v.type;
@@ -268,12 +279,21 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
                is_ju = ty == V_JULIA;
     const int ax = v.axis_x, ay = v.axis_y;
     const R x = coord<D>(t, ax), y = coord<D>(t, ay);
-    const R q = x * x + y * y;                          /* R2SQ */
-    R rt = R(0), ang = R(0), s = R(0), c = R(0), k = R(0);
-    if (present & (kTaHorseshoe | kTaPolar | kTaJulia))
-        rt = T::sqrt_(q);                               /* R2 */
-    if (present & (kTaPolar | kTaJulia))
-        ang = T::atan2_(y, x);
+    R q, rt = R(0), ang = R(0), s = R(0), c = R(0), k = R(0);
+    if (pp.valid)
+    {
+        q = pp.q;
+        rt = pp.rt;
+        ang = pp.ang;
+    }
+    else
+    {
+        q = x * x + y * y;                              /* R2SQ */
+        if (present & (kTaHorseshoe | kTaPolar | kTaJulia))
+            rt = T::sqrt_(q);                           /* R2 */
+        if (present & (kTaPolar | kTaJulia))
+            ang = T::atan2_(y, x);
+    }
     if (present & (kTaSwirl | kTaJulia))
     {
         R arg = q;                                      /* swirl 509-522: sincos(r^2) */
@@ -349,12 +369,12 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
 // src/rng/flame_rng.hpp).
 template <int D, typename R, typename Rng>
 __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng,
-                                          uint32_t present = ~0u)
+                                          uint32_t present, const PlanePrims<R>& pp)
 {
     using T = RealTraits<R>;
     if (tier_a(v.type))
     {
-        variation_tier_a<D, R>(v, t, o, rng, present);
+        variation_tier_a<D, R>(v, t, o, rng, present, pp);
         return;
     }
     const int ax = v.axis_x, ay = v.axis_y;
