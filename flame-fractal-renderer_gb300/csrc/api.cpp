@@ -1116,6 +1116,11 @@ struct ffr_batch
         size_t smem = 0;
         int grid = 0;
         cudaGraphExec_t exec = nullptr;
+        // claim order (interleave_chunks) of the last render's chunk counts
+        unsigned long long* d_order = nullptr;
+        unsigned long long* h_order = nullptr;  // pinned staging
+        size_t order_cap = 0;
+        std::vector<unsigned long long> order_chunks;
     };
     std::vector<Group> groups;
     uint64_t traj_len = 4096;               // samples per stream when not set per context
@@ -1152,12 +1157,69 @@ void batch_free(ffr_batch* b)
         cudaFree(g.d_jobs);
         if (g.h_jobs)
             cudaFreeHost(g.h_jobs);
+        cudaFree(g.d_order);
+        if (g.h_order)
+            cudaFreeHost(g.h_order);
     }
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream)
         cudaStreamDestroy(b->stream);
     delete b;
+}
+
+// (re)capture a group's graph: statistics/cursor reset, then the persistent
+// kernel over the group's job table and claim order
+cudaError_t batch_capture(ffr_batch* b, ffr_batch::Group& g)
+{
+    const Launchers& L = launchers(b->ctxs[g.members[0]]->opts.precision, g.dims);
+    if (g.exec)
+    {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    BatchArgs ba;
+    ba.jobs = g.d_jobs;
+    ba.njobs = (int)g.members.size();
+    ba.head = g.d_head;
+    ba.order = g.d_order;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return e;
+    cudaError_t e1 = launch_batch_reset(g.d_jobs, ba.njobs, g.d_head, b->stream);
+    cudaError_t e2 = L.batch(ba, g.color, g.grid, g.smem, b->stream);
+    e = cudaStreamEndCapture(b->stream, &graph);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess)
+    {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e);
+    }
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    return e;
+}
+
+// claim-order buffers with room for n entries
+cudaError_t batch_order_room(ffr_batch::Group& g, size_t n)
+{
+    if (n <= g.order_cap)
+        return cudaSuccess;
+    const size_t cap = std::max<size_t>(n, 2 * g.order_cap);
+    cudaFree(g.d_order);
+    g.d_order = nullptr;
+    if (g.h_order)
+        cudaFreeHost(g.h_order);
+    g.h_order = nullptr;
+    g.order_cap = 0;
+    g.order_chunks.clear();
+    cudaError_t e = cudaMalloc(&g.d_order, cap * sizeof(unsigned long long));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&g.h_order, cap * sizeof(unsigned long long), 0);
+    if (e == cudaSuccess)
+        g.order_cap = cap;
+    return e;
 }
 
 } // namespace
@@ -1242,27 +1304,12 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
         g.d_head = reinterpret_cast<BatchHead*>(g.d_jobs + nj);
         if ((e = cudaHostAlloc(&g.h_jobs, sizeof(JobDesc) * nj + sizeof(BatchHead), 0)) != cudaSuccess)
             return cfail(e, "cudaHostAlloc(job table)");
-        // capture: reset statistics + cursor, persistent kernel
-        BatchArgs ba;
-        ba.jobs = g.d_jobs;
-        ba.njobs = (int)nj;
-        ba.head = g.d_head;
-        cudaGraph_t graph = nullptr;
-        if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-            return cfail(e, "cudaStreamBeginCapture");
-        cudaError_t e1 = launch_batch_reset(g.d_jobs, (int)nj, g.d_head, b->stream);
-        cudaError_t e2 = L.batch(ba, g.color, g.grid, g.smem, b->stream);
-        e = cudaStreamEndCapture(b->stream, &graph);
-        if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess)
-        {
-            if (graph)
-                cudaGraphDestroy(graph);
-            return cfail(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e), "graph capture");
-        }
-        e = cudaGraphInstantiate(&g.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess)
-            return cfail(e, "cudaGraphInstantiate");
+        // capture: reset statistics + cursor, persistent kernel (recaptured
+        // when a render needs a larger claim order)
+        if ((e = batch_order_room(g, 4096)) != cudaSuccess)
+            return cfail(e, "claim order buffers");
+        if ((e = batch_capture(b, g)) != cudaSuccess)
+            return cfail(e, "graph capture");
     }
     *out = b;
     return FFR_OK;
@@ -1326,6 +1373,28 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
         BCU(b, cudaMemcpyAsync(g.d_jobs, g.h_jobs,
                                sizeof(JobDesc) * g.members.size() + sizeof(BatchHead),
                                cudaMemcpyHostToDevice, b->stream));
+        // interleaved claim order, rebuilt when the chunk counts change
+        std::vector<unsigned long long> counts(g.members.size());
+        for (size_t k = 0; k < g.members.size(); ++k)
+            counts[k] = g.h_jobs[k].chunks;
+        if (counts != g.order_chunks)
+        {
+            if (chunk > g.order_cap)
+            {
+                BCU(b, cudaStreamSynchronize(b->stream));
+                BCU(b, batch_order_room(g, chunk));
+                BCU(b, batch_capture(b, g));
+                BCU(b, cudaMemcpyAsync(g.d_jobs, g.h_jobs,
+                                       sizeof(JobDesc) * g.members.size() + sizeof(BatchHead),
+                                       cudaMemcpyHostToDevice, b->stream));
+            }
+            std::vector<unsigned long long> order;
+            interleave_chunks(counts, order);
+            std::memcpy(g.h_order, order.data(), order.size() * sizeof(unsigned long long));
+            BCU(b, cudaMemcpyAsync(g.d_order, g.h_order, order.size() * sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, b->stream));
+            g.order_chunks = counts;
+        }
     }
     BCU(b, cudaEventRecord(b->ev0, b->stream));
     for (auto& g : b->groups)

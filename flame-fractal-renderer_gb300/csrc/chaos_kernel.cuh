@@ -92,32 +92,47 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
 #pragma unroll
     for (int i = 0; i < D; ++i)
         v[i] = R(0);
-    // 2-D flames: the plane primitives of the benchmark variations, once
-    // per application (the same values every variation would compute)
-    PlanePrims<R> pp;
-    pp.valid = false;
-    pp.q = pp.rt = pp.ang = R(0);
-    if (D == 2 && (pg.present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
-    {
-        using T = RealTraits<R>;
-        const R px = t[0], py = t[D - 1];
-        pp.valid = true;
-        pp.q = px * px + py * py;
-        if (pg.present & (kTaHorseshoe | kTaPolar | kTaJulia))
-            pp.rt = T::sqrt_(pp.q);
-        if (pg.present & (kTaPolar | kTaJulia))
-            pp.ang = T::atan2_(py, px);
-    }
     const int vb = x.var_begin, ve = x.var_begin + x.var_count;
-    for (int k = vb; k < ve; ++k)
+    if (pg.present == kTaLinear)
     {
-        const VarT<R>& var = pg.var[k];
-        R o[D];
-        variation<D, R>(var, t, o, rng, pg.present, pp);
-        const R w = var.weight;
+        // every variation of the flame is linear (IFS fractals): v = sum of
+        // w_j * t in the reference's accumulation order, no dispatch
+        for (int k = vb; k < ve; ++k)
+        {
+            const R w = pg.var[k].weight;
 #pragma unroll
-        for (int i = 0; i < D; ++i)
-            v[i] += o[i] * w;
+            for (int i = 0; i < D; ++i)
+                v[i] += t[i] * w;
+        }
+    }
+    else
+    {
+        // 2-D flames: the plane primitives of the benchmark variations, once
+        // per application (the same values every variation would compute)
+        PlanePrims<R> pp;
+        pp.valid = false;
+        pp.q = pp.rt = pp.ang = R(0);
+        if (D == 2 && (pg.present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+        {
+            using T = RealTraits<R>;
+            const R px = t[0], py = t[D - 1];
+            pp.valid = true;
+            pp.q = px * px + py * py;
+            if (pg.present & (kTaHorseshoe | kTaPolar | kTaJulia))
+                pp.rt = T::sqrt_(pp.q);
+            if (pg.present & (kTaPolar | kTaJulia))
+                pp.ang = T::atan2_(py, px);
+        }
+        for (int k = vb; k < ve; ++k)
+        {
+            const VarT<R>& var = pg.var[k];
+            R o[D];
+            variation<D, R>(var, t, o, rng, pg.present, pp);
+            const R w = var.weight;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] += o[i] * w;
+        }
     }
     if (D < 3 || x.has_post)
         affine<D>(x.post, v, out);
@@ -562,7 +577,8 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(co
 }
 
 // Persistent multi-flame render: each CTA claims (job, chunk of BLOCK
-// streams) pairs from a global cursor until the job table is exhausted.  A
+// streams) pairs from a global cursor, in the claim order of b.order, until
+// the job table is exhausted.  A
 // job's streams are the ones ffr_render would run for that context alone,
 // so every job's buffer is the same alone and in the batch.  The claimed
 // job's arguments are copied to shared memory and its program is reloaded
@@ -584,17 +600,9 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_ker
             int j = -1;
             if (c < total)
             {
-                int lo = 0, hi = b.njobs - 1;
-                while (lo < hi)
-                {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (b.jobs[mid].chunk_begin <= c)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                j = lo;
-                s_chunk = c - b.jobs[j].chunk_begin + b.jobs[j].chunk_first;
+                const unsigned long long e = b.order[c];
+                j = (int)(e >> 32);
+                s_chunk = (e & 0xffffffffull) + b.jobs[j].chunk_first;
             }
             s_job = j;
         }

@@ -5,7 +5,10 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <functional>
+#include <queue>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "flame_program.h"
@@ -158,7 +161,47 @@ struct BatchArgs
     const JobDesc* jobs;
     int njobs;
     BatchHead* head;
+    // claim order: entry c = (job << 32) | chunk within the job's range,
+    // interleaved (interleave_chunks) so the CTAs running at any moment
+    // work on many jobs' buffers instead of one job's at a time
+    const unsigned long long* order;
 };
+
+// Claim order for jobs of chunks[k] chunks: chunk r of job k gets the key
+// (r + 1/2) / chunks[k] and claims run in ascending key order (ties by job),
+// so every job advances at the same relative pace and concurrent CTAs spread
+// over the jobs in proportion to their size.  (Binning every CTA into one
+// job's buffer at a time concentrates the L2 atomics: the 256-flame batch
+// ran 27% slower in job order.)  Any order gives the same buffers.
+inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
+                              std::vector<unsigned long long>& order)
+{
+    order.clear();
+    struct Item
+    {
+        double key;
+        unsigned long long job, r;
+        bool operator>(const Item& o) const
+        {
+            return key > o.key || (key == o.key && job > o.job);
+        }
+    };
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (size_t k = 0; k < chunks.size(); ++k)
+        if (chunks[k])
+            heap.push({0.5 / (double)chunks[k], k, 0});
+    while (!heap.empty())
+    {
+        Item it = heap.top();
+        heap.pop();
+        order.push_back((it.job << 32) | it.r);
+        if (++it.r < chunks[it.job])
+        {
+            it.key = ((double)it.r + 0.5) / (double)chunks[it.job];
+            heap.push(it);
+        }
+    }
+}
 
 // Single xform application on a batch of points (one stream per point).
 struct StepArgs

@@ -118,6 +118,9 @@ struct RoundSlot
     JobDesc* d_jobs = nullptr;          // capacity max_active
     BatchHead* d_heads = nullptr;       // kGroups
     JobDesc* h_jobs = nullptr;          // pinned mirror: jobs then heads
+    unsigned long long* d_order = nullptr;  // claim order of the round's chunks
+    unsigned long long* h_order = nullptr;  // pinned mirror
+    size_t order_cap = 0;
     bool busy = false;
     uint64_t started_ns = 0;
     std::vector<RoundPart> parts;
@@ -365,6 +368,7 @@ bool Server::launch_round_locked()
                                                         b0.smem);
         budget_chunks = 2ull * (uint64_t)sms * (uint64_t)std::max(1, bps);
     }
+    budget_chunks = std::min<uint64_t>(budget_chunks, r->order_cap);
     // even share, then what is left to the oldest jobs
     std::vector<uint64_t> take(cand.size(), 0);
     const uint64_t share = std::max<uint64_t>(1, budget_chunks / cand.size());
@@ -439,6 +443,24 @@ bool Server::launch_round_locked()
         hh[g].total_chunks = groups[g].chunks;
         hh[g].cursor = 0;
     }
+    // interleaved claim order per group (the round's chunks of many jobs)
+    size_t order_off[kGroups] = {};
+    size_t order_len = 0;
+    {
+        std::vector<unsigned long long> counts, ord;
+        for (int g = 0; g < kGroups; ++g)
+        {
+            order_off[g] = order_len;
+            if (!groups[g].n)
+                continue;
+            counts.assign(groups[g].n, 0);
+            for (int k = 0; k < groups[g].n; ++k)
+                counts[k] = r->h_jobs[groups[g].off + k].chunks;
+            interleave_chunks(counts, ord);
+            std::memcpy(r->h_order + order_len, ord.data(), ord.size() * sizeof(unsigned long long));
+            order_len += ord.size();
+        }
+    }
     cudaError_t e = cudaStreamWaitEvent(r->stream, ev_alloc, 0);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(r->d_jobs, r->h_jobs, sizeof(JobDesc) * nj, cudaMemcpyHostToDevice,
@@ -446,6 +468,9 @@ bool Server::launch_round_locked()
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(r->d_heads, hh, sizeof(BatchHead) * kGroups, cudaMemcpyHostToDevice,
                             r->stream);
+    if (e == cudaSuccess && order_len)
+        e = cudaMemcpyAsync(r->d_order, r->h_order, order_len * sizeof(unsigned long long),
+                            cudaMemcpyHostToDevice, r->stream);
     for (int g = 0; g < kGroups && e == cudaSuccess; ++g)
     {
         if (!groups[g].n)
@@ -466,6 +491,7 @@ bool Server::launch_round_locked()
         ba.jobs = r->d_jobs + groups[g].off;
         ba.njobs = groups[g].n;
         ba.head = r->d_heads + g;
+        ba.order = r->d_order + order_off[g];
         e = L.batch(ba, color, (int)grid, groups[g].smem, r->stream);
     }
     if (e == cudaSuccess)
@@ -711,6 +737,9 @@ void server_free(Server* s)
         cudaFree(r.d_jobs);
         if (r.h_jobs)
             cudaFreeHost(r.h_jobs);
+        cudaFree(r.d_order);
+        if (r.h_order)
+            cudaFreeHost(r.h_order);
         if (r.done)
             cudaEventDestroy(r.done);
         if (r.stream)
@@ -895,6 +924,13 @@ ffr_status ffr_server_create(const ffr_server_opts* opts, ffr_server** out)
         r.d_heads = reinterpret_cast<BatchHead*>(r.d_jobs + o.max_active);
         if ((e = cudaHostAlloc(&r.h_jobs, table, 0)) != cudaSuccess)
             return cfail(e, "cudaHostAlloc(job table)");
+        // the largest round: round_chunks, or two chunks for each of up to 16
+        // resident CTAs per SM
+        r.order_cap = std::max<size_t>(o.round_chunks, 2 * (size_t)s->sms * 16);
+        if ((e = cudaMalloc(&r.d_order, r.order_cap * sizeof(unsigned long long))) != cudaSuccess)
+            return cfail(e, "cudaMalloc(claim order)");
+        if ((e = cudaHostAlloc(&r.h_order, r.order_cap * sizeof(unsigned long long), 0)) != cudaSuccess)
+            return cfail(e, "cudaHostAlloc(claim order)");
     }
     size_t fr = 0, tot = 0;
     if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess)
