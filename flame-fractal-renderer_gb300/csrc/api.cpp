@@ -478,7 +478,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
     // static choice: FP32 plain, FP64 sorted where it fits (FP64 pays more
     // for divergent lanes)
     *kernel = c->opts.precision == FFR_FP64 ? FFR_KERNEL_AUTO : FFR_KERNEL_PLAIN;
-    *agg = 0;
+    *agg = kDefaultAgg;
     if (samples < kTuneMinSamples)
         return FFR_OK;
     const size_t cells = c->flame.cells;
@@ -819,7 +819,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         if (s != FFR_OK)
             return s;
     }
-    int kreq = c->opts.kernel, agg = 0;
+    int kreq = c->opts.kernel, agg = kDefaultAgg;
     if (kreq == FFR_KERNEL_AUTO)
     {
         ffr_status ts = autotune(c, samples, &kreq, &agg);
@@ -1361,7 +1361,7 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
                 return bfail(b, FFR_ERR_ARG, "too many samples per GPU thread (raise streams)");
             JobDesc& jd = g.h_jobs[k];
             fill_args(c, jd.a, N, seeds[g.members[k]], bad_limit, S, L, c->d_counts, c->d_hi,
-                      c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : 0);
+                      c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : kDefaultAgg);
             jd.chunk_begin = chunk;
             jd.chunks = (active + 127) / 128;
             jd.chunk_first = 0;

@@ -264,7 +264,21 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     const int rsl_words = a.rsl_words;
     uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + (16 + rsl_words) * BLOCK);
     unsigned long long* xfc_shared = reinterpret_cast<unsigned long long*>(xfc_local);
-    const bool local_xfc = nxf <= kLocalXfCounters;
+    const bool packed_xfc = nxf <= kPackedXfCounters;
+    const bool local_xfc = !packed_xfc && nxf <= kLocalXfCounters;
+    // packed: 8-bit per-xform fields of xpk, flushed every 255 samples
+    unsigned long long xpk = 0;
+    unsigned int xsince = 0;
+    auto xflush = [&]() __attribute__((always_inline)) {
+        for (int i = 0; i < nxf; ++i)
+        {
+            const unsigned int n = (unsigned int)(xpk >> (8 * i)) & 255u;
+            if (n)
+                atomicAdd(&xfc_shared[i], (unsigned long long)n);
+        }
+        xpk = 0;
+        xsince = 0;
+    };
     if (local_xfc)
     {
         for (int i = 0; i < nxf; ++i)
@@ -401,7 +415,13 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                             cf[i] = c[i];
                 }
                 ++s_iter;
-                if (local_xfc)
+                if (packed_xfc)
+                {
+                    xpk += 1ull << (8 * xi);
+                    if (++xsince == 255u)
+                        xflush();
+                }
+                else if (local_xfc)
                     ++xfc_local[xi * BLOCK + threadIdx.x];
                 else
                     atomicAdd(&xfc_shared[xi], 1ull);
@@ -534,6 +554,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 atomicMax(&a.stats->ext_hi[i], order_key(as_double(ext_hi[i])));
         }
     }
+    if (packed_xfc)
+        xflush();
     __syncthreads();
     if (local_xfc)
     {

@@ -12,7 +12,9 @@
 //   -t/--threads     accepted and echoed; the device decides its parallelism
 // Added options: --seed N (stream seeds; default from the clock, like the
 // reference's per-thread clock seeding), --precision fp64|fp32, --settle N
-// (default 53 = settle_iters<double>), --streams N, --device N,
+// (default 53 = settle_iters<double>), --streams N, --trajectories T (T
+// streams of one trajectory each, of ceil(samples / T) samples: "N samples
+// from T trajectories"; excludes -b and --streams), --device N,
 // --timeout-ms N.
 //
 // Errors: the reference lets parse/IO exceptions escape main (abort); this
@@ -50,6 +52,7 @@ struct Args
     int precision = FFR_FP64;
     uint64_t settle = 53;
     uint64_t streams = 0;
+    uint64_t trajectories = 0;
     int device = 0;
     uint64_t timeout_ms = 0;
     bool help = false;
@@ -70,6 +73,7 @@ const char* kUsage =
     "  --precision arg (=fp64)       fp64 (reference arithmetic) or fp32\n"
     "  --settle arg (=53)            settle iterations per trajectory\n"
     "  --streams arg (=0)            concurrent RNG streams (0 = device)\n"
+    "  --trajectories arg            trajectories (one stream each)\n"
     "  --device arg (=0)             CUDA device\n"
     "  --timeout-ms arg (=0)         render time limit (0 = none)\n";
 
@@ -100,7 +104,8 @@ Args parse_args(int argc, char** argv)
         {"output", 'o', true}, {"samples", 's', true}, {"threads", 't', true},
         {"batch-size", 'b', true}, {"bad-values", 'z', true},
         {"seed", 0, true}, {"precision", 0, true}, {"settle", 0, true},
-        {"streams", 0, true}, {"device", 0, true}, {"timeout-ms", 0, true},
+        {"streams", 0, true}, {"trajectories", 0, true}, {"device", 0, true},
+        {"timeout-ms", 0, true},
     };
     for (int k = 1; k < argc; ++k)
     {
@@ -164,6 +169,7 @@ Args parse_args(int argc, char** argv)
         }
         else if (n == "settle") a.settle = to_u64(val, n);
         else if (n == "streams") a.streams = to_u64(val, n);
+        else if (n == "trajectories") a.trajectories = to_u64(val, n);
         else if (n == "device") a.device = (int)to_u64(val, n);
         else if (n == "timeout-ms") a.timeout_ms = to_u64(val, n);
     }
@@ -201,6 +207,13 @@ int main(int argc, char** argv)
         die("the option '--flame' is required but missing");
     if (!a.have_output)
         die("the option '--output' is required but missing");
+    if (a.trajectories)
+    {
+        if (a.batch || a.streams)
+            die("--trajectories excludes --batch-size and --streams");
+        a.streams = a.trajectories;
+        a.batch = a.samples ? (a.samples + a.trajectories - 1) / a.trajectories : 1;
+    }
     if (!a.have_seed)
         a.seed = (uint64_t)std::chrono::steady_clock::now().time_since_epoch().count()
             ^ (uint64_t)std::chrono::system_clock::now().time_since_epoch().count();

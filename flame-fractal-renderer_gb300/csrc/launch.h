@@ -99,11 +99,17 @@ inline void set_geometry(RenderArgs& a, const void* prog, int precision)
     }
 }
 
+// xform counting in the render kernels: flames of up to kPackedXfCounters
+// xforms count in eight 8-bit fields of one register per thread (flushed
+// into per-CTA totals every 255 samples); up to kLocalXfCounters in per-thread
+// u32 counters in shared memory; beyond that in per-CTA u64 totals directly
+constexpr int kPackedXfCounters = 8;
 constexpr int kLocalXfCounters = 16;
-// ISAAC result array per render thread: one 16-word block, plus a second
-// 16 words carried across a refill ahead (isaac64.cuh) when the flame's
-// xforms draw different numbers of words (ProgHeader::draws_vary)
-constexpr int kIsaacRslMax = 32;
+// ISAAC result array per render thread: one 16-word block, plus up to 8
+// words carried across a refill ahead (isaac64.cuh) when the flame's xforms
+// draw different numbers of words (ProgHeader::draws_vary).  A carry of 8
+// (not 16) keeps such flames at 5 CTAs of 128 threads per SM.
+constexpr int kIsaacRslMax = 24;
 
 // result-array words for a program blob (16 or kIsaacRslMax)
 inline int rsl_words_for(const void* prog)
@@ -119,16 +125,16 @@ inline int rsl_words_for(const void* prog)
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
 
 // Dynamic shared memory of the plain and batch render kernels: the program,
-// ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), and
-// per-thread u32 xform counters when nxf <= kLocalXfCounters, else one u64
-// counter per xform for the CTA.
+// ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), and the
+// xform counters: per-thread u32 when kPackedXfCounters < nxf <=
+// kLocalXfCounters, else one u64 total per xform for the CTA.
 template <int BLOCK>
 __host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf,
                                                    int rsl_words)
 {
     size_t s = align16u(prog_bytes);
     s += (16 + (size_t)rsl_words) * (size_t)BLOCK * sizeof(uint64_t);
-    if (nxf <= kLocalXfCounters)
+    if (nxf > kPackedXfCounters && nxf <= kLocalXfCounters)
         s += (size_t)nxf * BLOCK * sizeof(uint32_t);
     else
         s += (size_t)nxf * sizeof(unsigned long long);
@@ -240,6 +246,13 @@ struct IsaacInit
 {
     unsigned long long w[16];
 };
+
+// Warp-merged binning (RenderArgs::agg) where no autotuner decision exists:
+// lanes of a warp that hit the same cell make one atomic add.  Flames with
+// hot cells (fixed points, dense cores) gain much more (the 1920x1080
+// benchmark flame: 30 G binned/s merged, 22 unmerged) than flames without
+// collisions lose (a match per sample).
+constexpr int kDefaultAgg = 1;
 
 // precision: 0 = FP64 mirror, 1 = FP32
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \

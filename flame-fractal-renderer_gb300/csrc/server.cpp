@@ -423,7 +423,7 @@ bool Server::launch_round_locked()
             a.stats = j->d_stats;
             a.cancel = d_cancel + j->slot;
             a.rng_words = b.rng_words;
-            a.agg = 0;
+            a.agg = kDefaultAgg;
             a.rsl_words = rsl_words_for(b.prog.data());
             std::memcpy(a.isaac_init, isaac_init, sizeof a.isaac_init);
             set_geometry(a, b.prog.data(), o.precision);
