@@ -305,7 +305,8 @@ def run_sierpinski(args):
     res = {}
     sampler = ClockSampler(dev)
     sampler.start()
-    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED}
+    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
+            "hot": ffr.KERNEL_HOT}
     for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
         with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
                                 device=dev, kernel=kern[args.kernel]) as r:
@@ -601,7 +602,7 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--max-active", type=int, default=256)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted", "hot"],
                     help="render kernel (auto: the library's autotuner decides)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -635,7 +636,8 @@ def main():
             dist.barrier()
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED}
+    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
+            "hot": ffr.KERNEL_HOT}
     r = ffr.BufferRenderer(text, precision=prec, settle=settle, device=local,
                            kernel=kern[args.kernel])
     for w in range(args.warmup):
@@ -658,7 +660,8 @@ def main():
         launches += 1
         streams, traj_len = s.streams, s.traj_len
         kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel) + (
-            " + warp-merged bins" if s.agg else "")
+            " + warp-merged bins" if s.agg else "") + (
+            f" + {s.hot_cells} hot cells in shared memory" if s.hot_cells else "")
     barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()

@@ -125,6 +125,13 @@ struct ffr_ctx
     bool tuned_spill = false;
     int tuned_kernel = FFR_KERNEL_PLAIN;
     int tuned_agg = 0;
+    bool tuned_hot = false;
+    bool hot_searched = false;      // FFR_KERNEL_HOT's probe has run
+    // hot-cell table of the plain kernel (kHotSlots keys), installed by the
+    // autotuner; hot_mult 0 = none
+    unsigned int* d_hot = nullptr;
+    unsigned int hot_mult = 0;
+    int hot_cells = 0;
     std::string err = "no error";
 
     const Launchers& L() const { return kLaunchers[opts.precision][flame.dims - 1]; }
@@ -243,6 +250,7 @@ void destroy(ffr_ctx* c)
     cudaFree(c->d_colors);
     cudaFree(c->d_stats);
     cudaFree(c->d_scratch);
+    cudaFree(c->d_hot);
     if (c->h_cancel)
         cudaFreeHost(c->h_cancel);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -263,9 +271,20 @@ int program_words(const ffr_ctx* c)
     return (int)h->rng_words_max;       // same offset in the float header
 }
 
+// Launch plan: kernel, streams, trajectory length and grid.  The hot-cell
+// table's shared memory is planned for FFR_KERNEL_HOT and when *hot is set
+// on entry, for the plain kernel with fewer than 2^30 cells and fewer than
+// 2^32 samples per CTA (the table's counts are u32); *hot on return: the
+// launch uses the context's table (planned and present).
 ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint64_t* L,
-                int* grid, int* kernel)
+                int* grid, int* kernel, bool* hot = nullptr)
 {
+    const bool want_hot = (kreq == FFR_KERNEL_HOT || (hot && *hot))
+        && c->flame.cells < (1ull << 30);
+    if (kreq == FFR_KERNEL_HOT)
+        kreq = FFR_KERNEL_PLAIN;
+    if (hot)
+        *hot = false;
     int bps = 0, block = 0;
     size_t smem = 0;
     const int color = c->flame.color_dims > 0, spill = c->d_hi != nullptr;
@@ -283,9 +302,10 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
         else
             k = FFR_KERNEL_PLAIN;
     }
+    const bool use_hot = want_hot && k == FFR_KERNEL_PLAIN;
     if (k == FFR_KERNEL_PLAIN)
-        CU(c, c->L().occ(color, rsl_words_for(c->prog_host.data()), &bps, &block, pb, nxf,
-                         &smem));
+        CU(c, c->L().occ(color, rsl_words_for(c->prog_host.data()), use_hot ? 1 : 0, &bps,
+                         &block, pb, nxf, &smem));
     *kernel = k;
     if (bps < 1)
         return fail(c, FFR_ERR_ARG, "render kernel does not fit on an SM "
@@ -308,9 +328,13 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     const long double per_thread = (long double)streams_per_thread * traj_per_stream * len;
     if (per_thread >= 4294967296.0L)
         return fail(c, FFR_ERR_ARG, "too many samples per GPU thread (raise streams)");
+    if (use_hot && per_thread * block >= 4294967296.0L)
+        return plan(c, samples, kreq, streams, L, grid, kernel, nullptr);
     *streams = S;
     *L = len;
     *grid = (int)blocks;
+    if (hot)
+        *hot = use_hot && c->hot_mult != 0;
     return FFR_OK;
 }
 
@@ -441,8 +465,15 @@ struct TuneKey
             < std::tie(o.prog, o.settle, o.streams, o.traj_len, o.spill, o.device);
     }
 };
+struct TuneChoice
+{
+    int kernel = FFR_KERNEL_PLAIN;
+    int agg = 0;
+    unsigned int hot_mult = 0;              // 0: no hot-cell table
+    std::vector<unsigned int> hot_keys;     // kHotSlots keys when hot_mult != 0
+};
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+std::map<TuneKey, TuneChoice> g_tune_cache;
 
 TuneKey tune_key(const ffr_ctx* c)
 {
@@ -450,28 +481,202 @@ TuneKey tune_key(const ffr_ctx* c)
                    c->opts.streams, c->opts.traj_len, c->d_hi != nullptr, c->device};
 }
 
+// candidates the hot-cell search collects at most per threshold
+constexpr unsigned int kHotCollectCap = 1024;
+
+// Hot-cell table from a probe's counts (u32, cells < 2^30): the up to
+// kHotCells cells holding at least 1/4096 of the probe's samples each, if
+// together they hold at least 1/50 of them, placed by a multiplier under
+// which no two keys share a slot.  On success *mult is odd and keys holds
+// kHotSlots entries (kHotEmpty where unused); *mult = 0 when the flame has
+// no such cells.  out: 1 + kHotCollectCap device words.
+ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long* out,
+                     unsigned int* mult, std::vector<unsigned int>& keys)
+{
+    *mult = 0;
+    const uint64_t cells = c->flame.cells;
+    if (cells >= (1ull << 30))
+        return FFR_OK;
+    unsigned long long init[3] = {0ull, ~0ull, 0ull}, red[3];
+    CU(c, cudaMemcpyAsync(out, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
+    CU(c, launch_hist_reduce(counts, nullptr, cells, out, c->stream));
+    CU(c, cudaMemcpyAsync(red, out, sizeof red, cudaMemcpyDeviceToHost, c->stream));
+    CU(c, cudaStreamSynchronize(c->stream));
+    const uint64_t sum = red[0];
+    if (sum < 4096)
+        return FFR_OK;
+    std::vector<unsigned long long> found;
+    for (uint64_t thr = sum >> 12; thr <= red[2]; thr *= 4)
+    {
+        CU(c, launch_hot_collect(counts, (unsigned int)cells,
+                                 (unsigned int)std::min<uint64_t>(thr, 0xFFFFFFFFull), out,
+                                 kHotCollectCap, c->stream));
+        unsigned long long n = 0;
+        CU(c, cudaMemcpyAsync(&n, out, sizeof n, cudaMemcpyDeviceToHost, c->stream));
+        CU(c, cudaStreamSynchronize(c->stream));
+        if (n > kHotCollectCap)
+            continue;           // too many at this threshold: raise it
+        found.resize(n);
+        if (n)
+        {
+            CU(c, cudaMemcpyAsync(found.data(), out + 1, n * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, c->stream));
+            CU(c, cudaStreamSynchronize(c->stream));
+        }
+        break;
+    }
+    // hottest first (ties by cell index, so the table is deterministic)
+    std::sort(found.begin(), found.end(), std::greater<unsigned long long>());
+    if (found.size() > (size_t)kHotCells)
+        found.resize(kHotCells);
+    uint64_t mass = 0;
+    for (unsigned long long f : found)
+        mass += f >> 32;
+    if (found.empty() || mass * 50 < sum)
+        return FFR_OK;
+    // odd multipliers from a fixed sequence until the keys land in distinct
+    // slots; with 64 keys in 256 slots about 1 in 4000 does, so give up on
+    // the coldest keys only after many tries
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    for (size_t n = found.size(); n >= 8; n -= 8)
+    {
+        for (int t = 0; t < 200000; ++t)
+        {
+            x = x * 6364136223846793005ull + 1442695040888963407ull;
+            const unsigned int m = (unsigned int)(x >> 32) | 1u;
+            uint64_t used[kHotSlots / 64] = {};
+            bool ok = true;
+            for (size_t i = 0; i < n && ok; ++i)
+            {
+                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
+                const unsigned int slot = (k * m) >> (32 - kHotSlotBits);
+                ok = !(used[slot / 64] >> (slot % 64) & 1);
+                used[slot / 64] |= 1ull << (slot % 64);
+            }
+            if (!ok)
+                continue;
+            keys.assign(kHotSlots, kHotEmpty);
+            for (size_t i = 0; i < n; ++i)
+            {
+                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
+                keys[(k * m) >> (32 - kHotSlotBits)] = k;
+            }
+            *mult = m;
+            return FFR_OK;
+        }
+        if (n < 16)
+            break;
+    }
+    return FFR_OK;
+}
+
+// install a hot-cell table (mult 0: none) on the context
+ffr_status set_hot(ffr_ctx* c, unsigned int mult, const std::vector<unsigned int>& keys)
+{
+    c->hot_mult = 0;
+    if (mult == 0)
+        return FFR_OK;
+    if (!c->d_hot)
+        CU(c, cudaMalloc(&c->d_hot, kHotSlots * sizeof(unsigned int)));
+    CU(c, cudaMemcpyAsync(c->d_hot, keys.data(), kHotSlots * sizeof(unsigned int),
+                          cudaMemcpyHostToDevice, c->stream));
+    CU(c, cudaStreamSynchronize(c->stream));
+    c->hot_mult = mult;
+    c->hot_cells = (int)std::count_if(keys.begin(), keys.end(),
+                                      [](unsigned int k) { return k != kHotEmpty; });
+    return FFR_OK;
+}
+
+// FFR_KERNEL_HOT: the context's hot-cell table from one probe render of the
+// plain kernel (2^24 samples, 2^22 in FP64) into scratch buffers, searched
+// once per context.
+ffr_status ensure_hot_table(ffr_ctx* c, uint64_t samples)
+{
+    if (c->hot_searched)
+        return FFR_OK;
+    c->hot_searched = true;
+    if (c->flame.cells >= (1ull << 30))
+        return FFR_OK;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t off_st = up(c->flame.cells * 4);
+    const size_t off_col = off_st + up(sizeof(DevStats));
+    const size_t r = (size_t)c->flame.color_dims;
+    const size_t off_hs = off_col + up(c->flame.cells * r * 8);
+    const size_t need = off_hs + (1 + kHotCollectCap) * sizeof(unsigned long long);
+    unsigned char* buf = nullptr;
+    CU(c, cudaMalloc(&buf, need));
+    CU(c, cudaMemsetAsync(buf, 0, c->flame.cells * 4, c->stream));
+    unsigned int* pc = reinterpret_cast<unsigned int*>(buf);
+    DevStats* pst = reinterpret_cast<DevStats*>(buf + off_st);
+    double* pcol = r ? reinterpret_cast<double*>(buf + off_col) : nullptr;
+    unsigned long long* phs = reinterpret_cast<unsigned long long*>(buf + off_hs);
+    const uint64_t P = std::max<uint64_t>(1, std::min<uint64_t>(
+        samples, c->opts.precision == FFR_FP64 ? (1u << 22) : (1u << 24)));
+    uint64_t S = 0, L = 0;
+    int grid = 0, kk = 0;
+    ffr_status st = plan(c, P, FFR_KERNEL_PLAIN, &S, &L, &grid, &kk);
+    if (st == FFR_OK)
+        st = reset_stats(c, pst);
+    if (st == FFR_OK)
+    {
+        RenderArgs a;
+        fill_args(c, a, P, 0x5eedull, ~0ull, S, L, pc, nullptr, pcol, pst, 1);
+        cudaError_t e = c->L().render(a, grid, c->stream);
+        if (e != cudaSuccess)
+            st = cuda_fail(c, e, "hot-cell probe");
+    }
+    unsigned int mult = 0;
+    std::vector<unsigned int> keys;
+    if (st == FFR_OK)
+        st = hot_table(c, pc, phs, &mult, keys);
+    if (st == FFR_OK)
+        st = set_hot(c, mult, keys);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(buf);
+    if (st == FFR_OK && e != cudaSuccess)
+        st = cuda_fail(c, e, "hot-cell probe");
+    return st;
+}
+
 // Autotuner: times a probe render of each (kernel, warp aggregation)
-// candidate into scratch buffers of the same geometry and keeps the fastest
-// for this context.  The probe never touches the context's buffer, so
-// results do not depend on whether tuning ran.
-ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
+// candidate into scratch buffers of the same geometry, then, if the probe
+// counts show hot cells, the plain kernel with a hot-cell table, and keeps
+// the fastest for this context.  The probe never touches the context's
+// buffer, so results do not depend on whether tuning ran.  *hot: use the
+// context's hot-cell table.
+ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* hot)
 {
     const bool spill = c->d_hi != nullptr;
+    *hot = false;
     if (c->tuned && c->tuned_spill == spill)
     {
         *kernel = c->tuned_kernel;
         *agg = c->tuned_agg;
+        *hot = c->tuned_hot;
         return FFR_OK;
     }
     {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        auto it = g_tune_cache.find(tune_key(c));
-        if (it != g_tune_cache.end())
+        TuneChoice ch;
+        bool have = false;
         {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(tune_key(c));
+            if (it != g_tune_cache.end())
+            {
+                ch = it->second;
+                have = true;
+            }
+        }
+        if (have)
+        {
+            ffr_status s = set_hot(c, ch.hot_mult, ch.hot_keys);
+            if (s != FFR_OK)
+                return s;
             c->tuned = true;
             c->tuned_spill = spill;
-            c->tuned_kernel = *kernel = it->second.first;
-            c->tuned_agg = *agg = it->second.second;
+            c->tuned_kernel = *kernel = ch.kernel;
+            c->tuned_agg = *agg = ch.agg;
+            c->tuned_hot = *hot = ch.hot_mult != 0;
             return FFR_OK;
         }
     }
@@ -483,14 +688,15 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
         return FFR_OK;
     const size_t cells = c->flame.cells;
     const size_t r = (size_t)c->flame.color_dims;
-    // scratch: counts | high words | colours | statistics, each 256-byte
-    // aligned (an odd cell count would otherwise leave the u64 fields of
-    // the statistics on a 4-byte boundary)
+    // scratch: counts | high words | colours | statistics | hot-cell
+    // search, each 256-byte aligned (an odd cell count would otherwise
+    // leave the u64 fields of the statistics on a 4-byte boundary)
     auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t off_hi = up(cells * 4);
     const size_t off_col = off_hi + (spill ? up(cells * 4) : 0);
     const size_t off_st = off_col + up(cells * r * 8);
-    const size_t need = off_st + sizeof(DevStats);
+    const size_t off_hs = off_st + up(sizeof(DevStats));
+    const size_t need = off_hs + (1 + kHotCollectCap) * sizeof(unsigned long long);
     size_t fr = 0, tot = 0;
     CU(c, cudaMemGetInfo(&fr, &tot));
     if (need > fr / 4)
@@ -501,71 +707,87 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg)
     unsigned int* ph = spill ? reinterpret_cast<unsigned int*>(buf + off_hi) : nullptr;
     double* pcol = r ? reinterpret_cast<double*>(buf + off_col) : nullptr;
     DevStats* pst = reinterpret_cast<DevStats*>(buf + off_st);
+    unsigned long long* phs = reinterpret_cast<unsigned long long*>(buf + off_hs);
     const uint64_t P = std::min<uint64_t>(samples, c->opts.precision == FFR_FP64 ? (1u << 22)
                                                                                  : (1u << 24));
     float best = 1e30f;
     int best_k = *kernel, best_a = 0;
+    bool best_h = false;
+    // one candidate: time two probe launches, keep the faster candidate
+    auto probe = [&](int k, int g, bool h) -> ffr_status {
+        uint64_t S = 0, L = 0;
+        int grid = 0, kk = 0;
+        bool hh = h;
+        if (plan(c, P, k, &S, &L, &grid, &kk, &hh) != FFR_OK || hh != h)
+            return FFR_OK;      // candidate does not apply to this flame
+        RenderArgs a;
+        fill_args(c, a, P, 0x5eedull + (uint64_t)k * 2 + g, ~0ull, S, L, pc, ph, pcol, pst, g);
+        if (h)
+        {
+            a.hot_keys = c->d_hot;
+            a.hot_mult = c->hot_mult;
+        }
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+            ffr_status st = reset_stats(c, pst);
+            if (st != FFR_OK)
+                return st;
+            CU(c, cudaEventRecord(c->ev0, c->stream));
+            CU(c, kk == FFR_KERNEL_SORTED ? c->L().sorted(a, grid, c->stream)
+                                          : c->L().render(a, grid, c->stream));
+            CU(c, cudaEventRecord(c->ev1, c->stream));
+            CU(c, cudaEventSynchronize(c->ev1));
+            CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        }
+        if (ms < best)
+        {
+            best = ms;
+            best_k = kk;
+            best_a = g;
+            best_h = h;
+        }
+        return FFR_OK;
+    };
     ffr_status st = FFR_OK;
     for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED})
-    {
         for (int g : {0, 1})
-        {
-            uint64_t S = 0, L = 0;
-            int grid = 0, kk = 0;
-            st = plan(c, P, k, &S, &L, &grid, &kk);
-            if (st != FFR_OK)
-            {
-                st = FFR_OK;        // candidate does not apply to this flame
-                continue;
-            }
-            RenderArgs a;
-            fill_args(c, a, P, 0x5eedull + (uint64_t)k * 2 + g, ~0ull, S, L, pc, ph, pcol,
-                      pst, g);
-            float ms = 0.f;
-            cudaError_t e = cudaSuccess;
-            for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep)
-            {
-                if ((st = reset_stats(c, pst)) != FFR_OK)
-                    break;
-                e = cudaEventRecord(c->ev0, c->stream);
-                if (e == cudaSuccess)
-                    e = kk == FFR_KERNEL_SORTED ? c->L().sorted(a, grid, c->stream)
-                                                : c->L().render(a, grid, c->stream);
-                if (e == cudaSuccess)
-                    e = cudaEventRecord(c->ev1, c->stream);
-                if (e == cudaSuccess)
-                    e = cudaEventSynchronize(c->ev1);
-                if (e == cudaSuccess)
-                    e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-            }
-            if (st != FFR_OK)
-                break;
-            if (e != cudaSuccess)
-            {
-                cudaFree(buf);
-                return cuda_fail(c, e, "autotune probe");
-            }
-            if (ms < best)
-            {
-                best = ms;
-                best_k = kk;
-                best_a = g;
-            }
-        }
-        if (st != FFR_OK)
-            break;
-    }
+            if (st == FFR_OK)
+                st = probe(k, g, false);
+    // the probes' counts (u32: far below 2^32 per cell) locate hot cells
+    unsigned int mult = 0;
+    std::vector<unsigned int> keys;
+    if (st == FFR_OK)
+        st = hot_table(c, pc, phs, &mult, keys);
+    if (st == FFR_OK)
+        st = set_hot(c, mult, keys);
+    if (st == FFR_OK && mult)
+        for (int g : {0, 1})
+            if (st == FFR_OK)
+                st = probe(FFR_KERNEL_PLAIN, g, true);
     cudaFree(buf);
     if (st != FFR_OK)
         return st;
+    if (!best_h)
+    {
+        c->hot_mult = 0;
+        mult = 0;
+        keys.clear();
+    }
     c->tuned = true;
     c->tuned_spill = spill;
     c->tuned_kernel = *kernel = best_k;
     c->tuned_agg = *agg = best_a;
+    c->tuned_hot = *hot = best_h;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     if (g_tune_cache.size() > 4096)
         g_tune_cache.clear();
-    g_tune_cache[tune_key(c)] = {best_k, best_a};
+    TuneChoice ch;
+    ch.kernel = best_k;
+    ch.agg = best_a;
+    ch.hot_mult = mult;
+    ch.hot_keys = std::move(keys);
+    g_tune_cache[tune_key(c)] = std::move(ch);
     return FFR_OK;
 }
 
@@ -604,7 +826,7 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: ABI version mismatch");
     if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown precision");
-    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_SORTED)
+    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_HOT)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown kernel");
     ffr_ctx* c = new (std::nothrow) ffr_ctx;
     if (!c)
@@ -794,6 +1016,26 @@ ffr_status ffr_plan(ffr_ctx* c, uint64_t samples, uint64_t* streams, uint64_t* t
     return FFR_OK;
 }
 
+namespace {
+
+// Before a render that could carry some count past 2^32 by the running bound
+// (every sample so far plus this render's), replace the bound by the exact
+// largest count, so that high words (and the slower returning atomics of
+// spill mode) are used only when a cell really can overflow.
+ffr_status tighten_bound(ffr_ctx* c, uint64_t samples)
+{
+    if (c->d_hi || c->count_bound + samples < 0xFFFFFFFFULL)
+        return FFR_OK;
+    uint64_t sum = 0, mn = 0, mx = 0;
+    ffr_status s = ffr_histogram(c, &sum, &mn, &mx);
+    if (s != FFR_OK)
+        return s;
+    c->count_bound = mx;
+    return FFR_OK;
+}
+
+} // namespace
+
 ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_limit,
                       ffr_stats* st)
 {
@@ -813,6 +1055,11 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     if (samples == 0)
         return FFR_OK;      // render(0) returns true (buffer_renderer.hpp:276-277)
     CU(c, cudaSetDevice(c->device));
+    {
+        ffr_status s = tighten_bound(c, samples);
+        if (s != FFR_OK)
+            return s;
+    }
     if (c->count_bound + samples >= 0xFFFFFFFFULL)
     {
         ffr_status s = ensure_hi(c);
@@ -820,15 +1067,22 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
             return s;
     }
     int kreq = c->opts.kernel, agg = kDefaultAgg;
+    bool hot = false;
     if (kreq == FFR_KERNEL_AUTO)
     {
-        ffr_status ts = autotune(c, samples, &kreq, &agg);
+        ffr_status ts = autotune(c, samples, &kreq, &agg, &hot);
+        if (ts != FFR_OK)
+            return ts;
+    }
+    else if (kreq == FFR_KERNEL_HOT)
+    {
+        ffr_status ts = ensure_hot_table(c, samples);
         if (ts != FFR_OK)
             return ts;
     }
     uint64_t S = 0, L = 0;
     int grid = 0, kernel = 0;
-    ffr_status s = plan(c, samples, kreq, &S, &L, &grid, &kernel);
+    ffr_status s = plan(c, samples, kreq, &S, &L, &grid, &kernel, &hot);
     if (s != FFR_OK)
         return s;
     if ((s = reset_stats(c, c->d_stats)) != FFR_OK)
@@ -836,6 +1090,14 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     RenderArgs a;
     fill_args(c, a, samples, seed, bad_limit, S, L, c->d_counts, c->d_hi, c->d_colors,
               c->d_stats, agg);
+    if (hot)
+    {
+        a.hot_keys = c->d_hot;
+        a.hot_mult = c->hot_mult;
+        // the table takes the collisions warp merging is for
+        if (c->opts.kernel == FFR_KERNEL_HOT)
+            a.agg = agg = 0;
+    }
     *c->h_cancel = 0u;
     CU(c, cudaEventRecord(c->ev0, c->stream));
     if (kernel == FFR_KERNEL_SORTED)
@@ -860,6 +1122,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->kernel_ms = ms;
         st->kernel = kernel;
         st->agg = agg;
+        st->hot_cells = hot ? c->hot_cells : 0;
     }
     if (hs.cancelled)
         return fail(c, FFR_ERR_TIMEOUT, "render cancelled");
@@ -1285,7 +1548,7 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
         {
             ffr_ctx* c = ctxs[m];
             size_t sm = 0;
-            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), &bps, &block,
+            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), 0, &bps, &block,
                            (unsigned int)c->prog_host.size(),
                            (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
                 return cfail(e, "occupancy");
@@ -1336,6 +1599,11 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
     for (size_t i = 0; i < n; ++i)
     {
         ffr_ctx* c = b->ctxs[i];
+        {
+            ffr_status s = tighten_bound(c, samples[i]);
+            if (s != FFR_OK)
+                return bfail(b, s, c->err);
+        }
         if (c->count_bound + samples[i] >= 0xFFFFFFFFULL)
         {
             ffr_status s = ensure_hi(c);

@@ -11,6 +11,8 @@
 //                      buffer_renderer.hpp:375-475
 //   launch_export      BufferRenderer::writeBuffer, buffer_renderer.hpp:476-480
 //   launch_hist_reduce histogramSum/Min/Max, buffer_renderer.hpp:483-507
+//   launch_hot_collect cells at or above a count (the render kernel's
+//                      hot-cell table; no reference counterpart)
 // All are grid-stride loops sized to the SM count: HBM-bound streaming.
 #include "isaac64.cuh"
 #include "launch.h"
@@ -282,6 +284,38 @@ cudaError_t launch_export(unsigned long long* file, unsigned long long cells,
 {
     export_kernel<<<grid_for(cells, 256), 256, 0, st>>>(file, cells, color_dims,
                                                          counts, hi, colors);
+    return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void hot_collect_kernel(const unsigned int* __restrict__ counts, unsigned int cells,
+                                   unsigned int thr, unsigned long long* out, unsigned int cap)
+{
+    // out[0]: number of cells found; out[1 ..]: (count << 32 | cell), the
+    // first cap of them in no particular order
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < cells;
+         i += gridDim.x * blockDim.x)
+    {
+        const unsigned int v = counts[i];
+        if (v >= thr)
+        {
+            const unsigned long long k = atomicAdd(out, 1ull);
+            if (k < cap)
+                out[1 + k] = ((unsigned long long)v << 32) | i;
+        }
+    }
+}
+
+} // namespace
+
+cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, unsigned int thr,
+                               unsigned long long* out, unsigned int cap, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess)
+        return e;
+    hot_collect_kernel<<<grid_for(cells, 256), 256, 0, st>>>(counts, cells, thr, out, cap);
     return cudaGetLastError();
 }
 

@@ -30,7 +30,8 @@ constexpr int kBlock = 128;
 template <bool C>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 {
-    const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf, a.rsl_words);
+    const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf, a.rsl_words,
+                                                 a.hot_keys != nullptr);
     auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -41,10 +42,10 @@ static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 }
 
 template <bool C>
-static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_words,
+static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_words, int hot,
                            size_t* smem_out)
 {
-    const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf, rsl_words);
+    const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf, rsl_words, hot != 0);
     auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -59,12 +60,12 @@ cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t 
     return a.color_dims > 0 ? launch_one<true>(a, grid, st) : launch_one<false>(a, grid, st);
 }
 
-cudaError_t FFR_NAME(occupancy)(int color, int rsl_words, int* blocks_per_sm, int* block,
-                                unsigned int prog_bytes, int nxf, size_t* smem)
+cudaError_t FFR_NAME(occupancy)(int color, int rsl_words, int hot, int* blocks_per_sm,
+                                int* block, unsigned int prog_bytes, int nxf, size_t* smem)
 {
     *block = kBlock;
-    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, smem)
-                 : occ_one<false>(blocks_per_sm, prog_bytes, nxf, rsl_words, smem);
+    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
+                 : occ_one<false>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
 }
 
 template <bool C>

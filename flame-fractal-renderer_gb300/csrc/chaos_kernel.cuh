@@ -215,37 +215,49 @@ template <> struct Geo<float>
 template <typename R>
 __device__ __forceinline__ double as_double(R x) { return (double)x; }
 
-// One count for cell bi.  With a.agg, lanes of the warp that bin the same
-// cell in this step are merged by __match_any_sync into one atomic add of
-// their number (hot cells: fixed points, dense attractor cores); otherwise
-// every lane issues its own fire-and-forget add.  With a.spill the returned
-// old value detects the u32 wrap and carries into the high word.
-__device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi)
+// n more counts for cell bi; with a.spill the returned old value detects
+// the u32 wrap and carries into the high word
+__device__ __forceinline__ void add_count(const RenderArgs& a, uint64_t bi, unsigned int n)
 {
+    if (a.spill)
+    {
+        const unsigned int old = atomicAdd(&a.counts[bi], n);
+        if (old + n < old)
+            atomicAdd(&a.hi[bi], 1u);
+    }
+    else
+        atomicAdd(&a.counts[bi], n);
+}
+
+// One count for cell bi.  A cell of the hot-cell table (hot: the CTA's
+// keys, then its counts, or null) counts in shared memory.  With a.agg,
+// lanes of the warp that bin the same cell in this step are merged by
+// __match_any_sync into one atomic add of their number (hot cells: fixed
+// points, dense attractor cores); otherwise every lane issues its own
+// fire-and-forget add.  With a.spill the returned old value detects the u32
+// wrap and carries into the high word.
+__device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi, unsigned int* hot)
+{
+    if (hot)
+    {
+        // the table needs fewer than 2^30 cells: bi fits 32 bits
+        const unsigned int k = (unsigned int)bi;
+        const unsigned int slot = (k * a.hot_mult) >> (32 - kHotSlotBits);
+        if (hot[slot] == k)
+        {
+            atomicAdd(&hot[kHotSlots + slot], 1u);
+            return;
+        }
+    }
     if (a.agg)
     {
         const unsigned int same = __match_any_sync(__activemask(), (unsigned long long)bi);
         if ((int)(threadIdx.x & 31u) != __ffs(same) - 1)
             return;
-        const unsigned int n = (unsigned int)__popc(same);
-        if (a.spill)
-        {
-            const unsigned int old = atomicAdd(&a.counts[bi], n);
-            if (old + n < old)
-                atomicAdd(&a.hi[bi], 1u);
-        }
-        else
-            atomicAdd(&a.counts[bi], n);
+        add_count(a, bi, (unsigned int)__popc(same));
         return;
     }
-    if (a.spill)
-    {
-        const unsigned int old = atomicAdd(&a.counts[bi], 1u);
-        if (old == 0xFFFFFFFFu)
-            atomicAdd(&a.hi[bi], 1u);
-    }
-    else
-        atomicAdd(&a.counts[bi], 1u);
+    add_count(a, bi, 1u);
 }
 
 // Runs streams s_first, s_first + s_stride, ... (below the job's active
@@ -305,6 +317,20 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 && (int)rng.cnt <= rsl_words - 16)
             rng.refill();
     };
+
+    // hot-cell table: keys from a.hot_keys, counts zeroed
+    unsigned int* hot = nullptr;
+    if (a.hot_keys)
+    {
+        hot = reinterpret_cast<unsigned int*>(smem + chaos_smem_bytes<BLOCK>(a.prog_bytes, nxf,
+                                                                             rsl_words));
+        for (int i = threadIdx.x; i < kHotSlots; i += BLOCK)
+        {
+            hot[i] = a.hot_keys[i];
+            hot[kHotSlots + i] = 0u;
+        }
+        __syncthreads();
+    }
 
     // per-thread counters fit 32 bits: a thread runs fewer than 2^32
     // samples (checked by the launch planners)
@@ -497,7 +523,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     }
                     if (bi < a.cells)
                     {
-                        bin_count(a, bi);
+                        bin_count(a, bi, hot);
                         if (COLOR)
                             for (int i = 0; i < r; ++i)
                                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));
@@ -557,6 +583,17 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     if (packed_xfc)
         xflush();
     __syncthreads();
+    // the CTA's hot-cell counts (below 2^32: the planner bounds a CTA's
+    // samples) into the buffer
+    if (hot)
+    {
+        for (int i = threadIdx.x; i < kHotSlots; i += BLOCK)
+        {
+            const unsigned int n = hot[kHotSlots + i];
+            if (n)
+                add_count(a, hot[i], n);
+        }
+    }
     if (local_xfc)
     {
         for (int i = 0; i < nxf; ++i)

@@ -310,7 +310,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             ++dropped;
             return;
         }
-        bin_count(a, bi);
+        bin_count(a, bi, nullptr);
         if (COLOR)
             for (int i = 0; i < r; ++i)
                 atomicAdd(&a.colors[bi * r + i], as_double(cf[i]));

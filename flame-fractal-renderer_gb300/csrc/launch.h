@@ -55,6 +55,10 @@ struct RenderArgs
     int rng_words;                  // largest RNG draw of one xform (sorted kernel)
     int agg;                        // warp-aggregate increments of equal cells
     int rsl_words;                  // ISAAC result array words (16 or kIsaacRslMax)
+    // hot-cell table of the plain kernel (kHotSlots keys), or null; needs
+    // fewer than 2^30 cells and fewer than 2^32 samples per CTA
+    const unsigned int* hot_keys;
+    unsigned int hot_mult;
     unsigned long long isaac_init[16];
     // the program header's geometry, copied here so the render loop reads
     // it from kernel parameters instead of shared memory each sample
@@ -124,13 +128,28 @@ inline int rsl_words_for(const void* prog)
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
 
+// Hot cells: a flame's density can sit largely in a few cells (fixed
+// points, attractor cores; the 1920x1080 benchmark flame puts 18% of its
+// samples in 64 cells and 5.5% in one 128-byte line), and atomic adds on
+// those few L2 lines then cap the binning rate.  The plain render kernel can
+// count up to kHotCells such cells per CTA in shared memory: a direct-mapped
+// table of kHotSlots keys (slot = (cell * hot_mult) >> (32 - kHotSlotBits),
+// the multiplier chosen so that the keys do not collide; empty slots hold
+// kHotEmpty) and their u32 counts, added to the buffer once when the CTA
+// ends.
+constexpr int kHotSlotBits = 8;
+constexpr int kHotSlots = 1 << kHotSlotBits;
+constexpr int kHotCells = 64;
+constexpr unsigned int kHotEmpty = 0xFFFFFFFFu;
+
 // Dynamic shared memory of the plain and batch render kernels: the program,
-// ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), and the
-// xform counters: per-thread u32 when kPackedXfCounters < nxf <=
-// kLocalXfCounters, else one u64 total per xform for the CTA.
+// ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), the
+// xform counters (per-thread u32 when kPackedXfCounters < nxf <=
+// kLocalXfCounters, else one u64 total per xform for the CTA), and with hot
+// the hot-cell table (kHotSlots keys, then kHotSlots counts).
 template <int BLOCK>
 __host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int nxf,
-                                                   int rsl_words)
+                                                   int rsl_words, bool hot = false)
 {
     size_t s = align16u(prog_bytes);
     s += (16 + (size_t)rsl_words) * (size_t)BLOCK * sizeof(uint64_t);
@@ -138,6 +157,8 @@ __host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int 
         s += (size_t)nxf * BLOCK * sizeof(uint32_t);
     else
         s += (size_t)nxf * sizeof(unsigned long long);
+    if (hot)
+        s += 2 * (size_t)kHotSlots * sizeof(uint32_t);
     return s;
 }
 
@@ -258,9 +279,10 @@ constexpr int kDefaultAgg = 1;
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \
     cudaError_t launch_render_p##P##_d##D(const RenderArgs&, int grid,          \
                                           cudaStream_t);                        \
-    cudaError_t occupancy_p##P##_d##D(int color, int rsl_words, int* blocks_per_sm, \
-                                      int* block, unsigned int prog_bytes,      \
-                                      int nxf, size_t* smem);                   \
+    cudaError_t occupancy_p##P##_d##D(int color, int rsl_words, int hot,        \
+                                      int* blocks_per_sm, int* block,           \
+                                      unsigned int prog_bytes, int nxf,         \
+                                      size_t* smem);                            \
     cudaError_t launch_sorted_p##P##_d##D(const RenderArgs&, int grid,          \
                                           cudaStream_t);                        \
     cudaError_t occupancy_sorted_p##P##_d##D(int color, int spill,              \
@@ -282,7 +304,7 @@ FFR_DECLARE_LAUNCHERS(1, 2)
 FFR_DECLARE_LAUNCHERS(1, 3)
 
 typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
-typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
+typedef cudaError_t (*OccFn)(int, int, int, int*, int*, unsigned int, int, size_t*);
 typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
 typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
 typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
@@ -321,6 +343,11 @@ cudaError_t launch_file_max(const unsigned long long* file, unsigned long long c
 cudaError_t launch_hist_reduce(const unsigned int* counts, const unsigned int* hi,
                                unsigned long long cells, unsigned long long* out,
                                cudaStream_t);
+
+// cells with count >= thr: out[0] = how many, out[1 ..] = (count << 32 |
+// cell) for the first cap of them (out holds 1 + cap words)
+cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, unsigned int thr,
+                               unsigned long long* out, unsigned int cap, cudaStream_t);
 
 cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned int iters,
                                int grid, int block, unsigned int salt, cudaStream_t);

@@ -91,9 +91,6 @@ ffr_status scratch_for(int device, unsigned char** out)
     return FFR_OK;
 }
 
-typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
-typedef cudaError_t (*OccFn)(int, int, int*, int*, unsigned int, int, size_t*);
-
 void pick_launchers(int precision, int dims, RenderFn* r, OccFn* o)
 {
     static const RenderFn rf[2][3] = {
@@ -177,7 +174,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     const int nxf = (int)f.xforms.size();
     int bps = 0, block = 0, sms = 1;
     size_t smem = 0;
-    if ((e = occ(f.color_dims > 0, rsl_words_for(prog.data()), &bps, &block,
+    if ((e = occ(f.color_dims > 0, rsl_words_for(prog.data()), 0, &bps, &block,
                  (unsigned int)prog.size(), nxf, &smem))
             != cudaSuccess)
         return nocuda(e, "occupancy");

@@ -151,6 +151,7 @@ struct Server
     std::mutex rd_mu;
     std::condition_variable rd_cv;
     cudaEvent_t ev_alloc = nullptr;     // after the latest admission work
+    unsigned long long* d_red = nullptr;    // 3 words: histogram sum, min, max
     unsigned int* h_cancel = nullptr;   // mapped pinned flags, one per slot
     unsigned int* d_cancel = nullptr;
     std::vector<int> free_slots;
@@ -249,6 +250,23 @@ void Server::admit_locked()
             queue.pop_front();
             fail_job_locked(j, FFR_ERR_OOM);
             continue;
+        }
+        if (!b.d_hi && b.allocated && b.running == 0 && b.count_bound + j->samples >= 0xFFFFFFFFULL)
+        {
+            // the bound counts every sample rendered so far; replace it by
+            // the exact largest count before deciding on high words
+            unsigned long long init[3] = {0ull, ~0ull, 0ull}, out[3] = {0ull, 0ull, 0ull};
+            cudaError_t er = cudaMemcpyAsync(d_red, init, sizeof init, cudaMemcpyHostToDevice, aux);
+            if (er == cudaSuccess)
+                er = launch_hist_reduce(b.d_counts, nullptr, b.flame.cells, d_red, aux);
+            if (er == cudaSuccess)
+                er = cudaMemcpyAsync(out, d_red, sizeof out, cudaMemcpyDeviceToHost, aux);
+            if (er == cudaSuccess)
+                er = cudaStreamSynchronize(aux);
+            if (er == cudaSuccess)
+                b.count_bound = out[2];
+            else
+                cudaGetLastError();
         }
         const bool need_hi = b.count_bound + j->samples >= 0xFFFFFFFFULL && !b.d_hi;
         // counts of jobs already running on this buffer carry no high words
@@ -768,6 +786,7 @@ void server_free(Server* s)
     }
     if (s->ev_alloc)
         cudaEventDestroy(s->ev_alloc);
+    cudaFree(s->d_red);
     if (s->h_cancel)
         cudaFreeHost(s->h_cancel);
     if (s->pool)
@@ -904,6 +923,8 @@ ffr_status ffr_server_create(const ffr_server_opts* opts, ffr_server** out)
         return cfail(e, "cudaEventCreate");
     if ((e = cudaEventRecord(s->ev_alloc, s->aux)) != cudaSuccess)
         return cfail(e, "cudaEventRecord");
+    if ((e = cudaMalloc(&s->d_red, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return cfail(e, "cudaMalloc(reduction)");
     if ((e = cudaHostAlloc(&s->h_cancel, sizeof(unsigned int) * o.max_active,
                            cudaHostAllocMapped)) != cudaSuccess)
         return cfail(e, "cudaHostAlloc(cancel flags)");

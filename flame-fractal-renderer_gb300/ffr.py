@@ -31,7 +31,7 @@ STATUS_NAMES = ["FFR_OK", "FFR_BAD_VALUES", "FFR_ERR_PARSE", "FFR_ERR_ARG",
                 "FFR_ERR_IO", "FFR_ERR_OOM", "FFR_ERR_TIMEOUT", "FFR_ERR_CUDA",
                 "FFR_ERR_STATE"]
 FP64, FP32 = 0, 1
-KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED = 0, 1, 2
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED, KERNEL_HOT = 0, 1, 2, 3
 
 # every symbol include/ffr_gpu.h declares
 EXPORTS = [
@@ -81,7 +81,8 @@ class Stats(ctypes.Structure):
                 ("bad_pts", (ctypes.c_double * MAX_DIMS) * MAX_BAD_RECORDS),
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
-                ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32)]
+                ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32),
+                ("hot_cells", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class ImageInfo(ctypes.Structure):
@@ -213,6 +214,7 @@ class RenderStats:
     kernel_ms: float
     kernel: int
     agg: int
+    hot_cells: int = 0
 
     @property
     def ok(self) -> bool:
@@ -230,7 +232,7 @@ def _render_stats(status: int, st: Stats, n: int) -> RenderStats:
         bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
         bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
         streams=st.streams, traj_len=st.traj_len, settle=st.settle,
-        kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg)
+        kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg, hot_cells=st.hot_cells)
 
 
 def isaac_words(key: int, n: int, device: int = 0) -> np.ndarray:

@@ -82,7 +82,14 @@ typedef struct ffr_opts {
 #define FFR_MAX_XFORM_IDS 4096
 #define FFR_MAX_BAD_RECORDS 4096
 
-enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2 };
+/* Render kernel (ffr_opts.kernel).  AUTO: autotuned for renders of 2^25
+   samples and more (plain or xform-sorted, warp-merged binning or not, hot-
+   cell table or not), else plain (FP32) or sorted where it fits (FP64).
+   HOT: the plain kernel counting the flame's hottest cells (found by one
+   probe render) in per-CTA shared memory, without warp merging; streams
+   are planned with that memory reserved.  All choices give identical buffers for equal streams
+   and trajectory lengths. */
+enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2, FFR_KERNEL_HOT = 3 };
 
 typedef struct ffr_stats {
     uint64_t samples_iterated;   /* getSamplesIterated */
@@ -104,6 +111,9 @@ typedef struct ffr_stats {
     double kernel_ms;            /* device time of the render kernel(s) */
     int32_t kernel;              /* FFR_KERNEL_PLAIN or FFR_KERNEL_SORTED */
     int32_t agg;                 /* 1: equal-cell increments were warp-merged */
+    int32_t hot_cells;           /* cells counted in per-CTA shared memory
+                                    (the autotuner's hot-cell table), or 0 */
+    int32_t reserved;
 } ffr_stats;
 
 typedef struct ffr_ctx ffr_ctx;
