@@ -412,6 +412,7 @@ def run_batch256(args):
             ms += sts[0].kernel_ms
             binned += sum(st.samples_plotted - st.dropped for st in sts)
         clocks = sampler.stop()
+        nhot = sum(1 for st in sts if st.hot_cells)
     for r in rs:
         r.close()
     value = binned / (ms * 1e-3)
@@ -425,6 +426,7 @@ def run_batch256(args):
           "in one persistent launch", value, ms / args.steps, "f32",
           {"flames": len(texts), "samples_per_step": sum(ns), "settle": 20, "seed": 11,
            "traj_len": 4096, "kernel": "persistent batch (CUDA graph)",
+           "hot_cell_tables": f"{nhot} of {len(texts)} jobs",
            "flush": "256 MiB L2 flush between timed steps"},
           gpu_launches=args.steps * 2,
           tv={"per_flame": tvs,

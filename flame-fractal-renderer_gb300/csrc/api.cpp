@@ -587,9 +587,9 @@ ffr_status set_hot(ffr_ctx* c, unsigned int mult, const std::vector<unsigned int
     return FFR_OK;
 }
 
-// FFR_KERNEL_HOT: the context's hot-cell table from one probe render of the
-// plain kernel (2^24 samples, 2^22 in FP64) into scratch buffers, searched
-// once per context.
+// The context's hot-cell table from one probe render of the plain kernel
+// (samples, at most 2^24 and 2^22 in FP64) into scratch buffers, searched
+// once per context (FFR_KERNEL_HOT renders, batch members).
 ffr_status ensure_hot_table(ffr_ctx* c, uint64_t samples)
 {
     if (c->hot_searched)
@@ -1384,9 +1384,13 @@ struct ffr_batch
         unsigned long long* h_order = nullptr;  // pinned staging
         size_t order_cap = 0;
         std::vector<unsigned long long> order_chunks;
+        // members whose hot-cell table the shared memory was sized for
+        std::vector<char> hot;
     };
     std::vector<Group> groups;
     uint64_t traj_len = 4096;               // samples per stream when not set per context
+    std::vector<int> job_hot;               // last render: hot-cell table cells per job
+    std::vector<int> job_agg;               // last render: warp merging per job
     std::string err = "no error";
 };
 
@@ -1547,8 +1551,21 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
         for (int m : g.members)
         {
             ffr_ctx* c = ctxs[m];
+            // hot-cell table from a 2^20-sample probe for autotuned and
+            // FFR_KERNEL_HOT members
+            if (c->opts.kernel == FFR_KERNEL_AUTO || c->opts.kernel == FFR_KERNEL_HOT)
+            {
+                if (ensure_hot_table(c, 1u << 20) != FFR_OK)
+                {
+                    std::string m2 = "hot-cell probe: " + c->err;
+                    batch_free(b);
+                    return fail(nullptr, FFR_ERR_CUDA, m2);
+                }
+            }
+            const int hot = c->hot_mult != 0;
+            g.hot.push_back((char)hot);
             size_t sm = 0;
-            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), 0, &bps, &block,
+            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), hot, &bps, &block,
                            (unsigned int)c->prog_host.size(),
                            (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
                 return cfail(e, "occupancy");
@@ -1595,6 +1612,8 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
         return FFR_ERR_ARG;
     BCU(b, cudaSetDevice(b->device));
     const size_t n = b->ctxs.size();
+    b->job_hot.assign(n, 0);
+    b->job_agg.assign(n, 0);
     // streams and trajectory length per job, high-word planes where needed
     for (size_t i = 0; i < n; ++i)
     {
@@ -1630,6 +1649,19 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
             JobDesc& jd = g.h_jobs[k];
             fill_args(c, jd.a, N, seeds[g.members[k]], bad_limit, S, L, c->d_counts, c->d_hi,
                       c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : kDefaultAgg);
+            // the hot-cell table where the shared memory was sized for it and
+            // a chunk (128 streams) stays below 2^32 samples (u32 counts)
+            const int i = g.members[k];
+            b->job_hot[i] = 0;
+            if (g.hot[k] && c->hot_mult
+                && (long double)((ntraj + S - 1) / S) * L * 128 < 4294967296.0L)
+            {
+                jd.a.hot_keys = c->d_hot;
+                jd.a.hot_mult = c->hot_mult;
+                jd.a.agg = 0;
+                b->job_hot[i] = c->hot_cells;
+            }
+            b->job_agg[i] = jd.a.agg;
             jd.chunk_begin = chunk;
             jd.chunks = (active + 127) / 128;
             jd.chunk_first = 0;
@@ -1688,6 +1720,8 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
             return bfail(b, s, c->err);
         st->kernel_ms = ms;
         st->kernel = FFR_KERNEL_PLAIN;
+        st->agg = b->job_agg[i];
+        st->hot_cells = b->job_hot[i];
     }
     return worst;
 }

@@ -301,7 +301,7 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
         {
             R bit = R(0);
             if (is_ju)                                  /* julia 807-819: randBool */
-                bit = (R)(rng.next() & 1u);
+                bit = (rng.next() & 1u) ? R(1) : R(0);
             const R ja = R(0.5) * ang + bit * T::pi;
             arg = is_ju ? ja : arg;
         }
@@ -553,7 +553,7 @@ __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rn
         X = m0 + m1; Y = m0 - m1; break;
     }
     case V_JULIA: /* 807-819 */
-        a = R(0.5) * T::atan2_(y, x) + (R)(rng.next() & 1u) * T::pi;
+        a = R(0.5) * T::atan2_(y, x) + ((rng.next() & 1u) ? R(1) : R(0)) * T::pi;
         T::sincos_(a, &s, &c);
         r = R2;
         X = c * r; Y = s * r; break;

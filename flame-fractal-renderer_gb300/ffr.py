@@ -440,7 +440,8 @@ class Batch:
                 xf_dist=np.array(st.xf_dist[:min(int(st.xform_ids), MAX_XFORM_IDS)], dtype=np.uint64),
                 bad_xf=np.array(st.bad_xf[:st.bad_recorded], dtype=np.uint64),
                 bad_pts=np.zeros((0, d)), streams=st.streams, traj_len=st.traj_len,
-                settle=st.settle, kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg))
+                settle=st.settle, kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg,
+                hot_cells=st.hot_cells))
         return status, out
 
     def close(self):

@@ -56,6 +56,8 @@ def test_batch_equals_solo(ffr, flames, precision):
         assert st.samples_iterated == ws.samples_iterated == n
         assert st.samples_plotted == ws.samples_plotted
         assert st.xf_dist.tolist() == ws.xf_dist.tolist()
+    # the random flame has hot cells: its job counted them in shared memory
+    assert sts[5].hot_cells > 0 and sts[5].agg == 0
     for r in rs:
         r.close()
 
