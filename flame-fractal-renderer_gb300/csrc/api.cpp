@@ -99,6 +99,54 @@ const Launchers& ffr::launchers(int precision, int dims)
     return kLaunchers[precision][dims - 1];
 }
 
+bool ffr::hot_place(std::vector<unsigned long long>& found, unsigned long long sum,
+                    unsigned int* mult, std::vector<unsigned int>& keys)
+{
+    // hottest first (ties by cell index, so the table is deterministic)
+    std::sort(found.begin(), found.end(), std::greater<unsigned long long>());
+    if (found.size() > (size_t)kHotCells)
+        found.resize(kHotCells);
+    unsigned long long mass = 0;
+    for (unsigned long long f : found)
+        mass += f >> 32;
+    if (found.empty() || mass * 50 < sum)
+        return false;
+    // odd multipliers from a fixed sequence until the keys land in distinct
+    // slots; with 64 keys in 256 slots about 1 in 4000 does, so give up on
+    // the coldest keys only after many tries
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    for (size_t n = found.size(); n >= 8; n -= 8)
+    {
+        for (int t = 0; t < 200000; ++t)
+        {
+            x = x * 6364136223846793005ull + 1442695040888963407ull;
+            const unsigned int m = (unsigned int)(x >> 32) | 1u;
+            uint64_t used[kHotSlots / 64] = {};
+            bool ok = true;
+            for (size_t i = 0; i < n && ok; ++i)
+            {
+                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
+                const unsigned int slot = (k * m) >> (32 - kHotSlotBits);
+                ok = !(used[slot / 64] >> (slot % 64) & 1);
+                used[slot / 64] |= 1ull << (slot % 64);
+            }
+            if (!ok)
+                continue;
+            keys.assign(kHotSlots, kHotEmpty);
+            for (size_t i = 0; i < n; ++i)
+            {
+                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
+                keys[(k * m) >> (32 - kHotSlotBits)] = k;
+            }
+            *mult = m;
+            return true;
+        }
+        if (n < 16)
+            break;
+    }
+    return false;
+}
+
 struct ffr_ctx
 {
     ffr_opts opts{};
@@ -481,15 +529,10 @@ TuneKey tune_key(const ffr_ctx* c)
                    c->opts.streams, c->opts.traj_len, c->d_hi != nullptr, c->device};
 }
 
-// candidates the hot-cell search collects at most per threshold
-constexpr unsigned int kHotCollectCap = 1024;
-
-// Hot-cell table from a probe's counts (u32, cells < 2^30): the up to
-// kHotCells cells holding at least 1/4096 of the probe's samples each, if
-// together they hold at least 1/50 of them, placed by a multiplier under
-// which no two keys share a slot.  On success *mult is odd and keys holds
-// kHotSlots entries (kHotEmpty where unused); *mult = 0 when the flame has
-// no such cells.  out: 1 + kHotCollectCap device words.
+// Hot-cell table from a probe's counts (u32, cells < 2^30): candidates
+// holding at least 1/4096 of the probe's samples each, placed by
+// hot_place; *mult = 0 when the flame has no such cells.  out: 1 +
+// kHotCollectCap device words.
 ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long* out,
                      unsigned int* mult, std::vector<unsigned int>& keys)
 {
@@ -525,48 +568,8 @@ ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long*
         }
         break;
     }
-    // hottest first (ties by cell index, so the table is deterministic)
-    std::sort(found.begin(), found.end(), std::greater<unsigned long long>());
-    if (found.size() > (size_t)kHotCells)
-        found.resize(kHotCells);
-    uint64_t mass = 0;
-    for (unsigned long long f : found)
-        mass += f >> 32;
-    if (found.empty() || mass * 50 < sum)
-        return FFR_OK;
-    // odd multipliers from a fixed sequence until the keys land in distinct
-    // slots; with 64 keys in 256 slots about 1 in 4000 does, so give up on
-    // the coldest keys only after many tries
-    uint64_t x = 0x9E3779B97F4A7C15ull;
-    for (size_t n = found.size(); n >= 8; n -= 8)
-    {
-        for (int t = 0; t < 200000; ++t)
-        {
-            x = x * 6364136223846793005ull + 1442695040888963407ull;
-            const unsigned int m = (unsigned int)(x >> 32) | 1u;
-            uint64_t used[kHotSlots / 64] = {};
-            bool ok = true;
-            for (size_t i = 0; i < n && ok; ++i)
-            {
-                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
-                const unsigned int slot = (k * m) >> (32 - kHotSlotBits);
-                ok = !(used[slot / 64] >> (slot % 64) & 1);
-                used[slot / 64] |= 1ull << (slot % 64);
-            }
-            if (!ok)
-                continue;
-            keys.assign(kHotSlots, kHotEmpty);
-            for (size_t i = 0; i < n; ++i)
-            {
-                const unsigned int k = (unsigned int)(found[i] & 0xFFFFFFFFull);
-                keys[(k * m) >> (32 - kHotSlotBits)] = k;
-            }
-            *mult = m;
-            return FFR_OK;
-        }
-        if (n < 16)
-            break;
-    }
+    if (!hot_place(found, sum, mult, keys))
+        *mult = 0;
     return FFR_OK;
 }
 

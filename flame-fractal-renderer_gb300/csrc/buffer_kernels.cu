@@ -289,11 +289,12 @@ cudaError_t launch_export(unsigned long long* file, unsigned long long cells,
 
 namespace {
 
-__global__ void hot_collect_kernel(const unsigned int* __restrict__ counts, unsigned int cells,
+__global__ void hot_collect_kernel(const volatile unsigned int* counts, unsigned int cells,
                                    unsigned int thr, unsigned long long* out, unsigned int cap)
 {
     // out[0]: number of cells found; out[1 ..]: (count << 32 | cell), the
-    // first cap of them in no particular order
+    // first cap of them in no particular order.  Volatile loads are relaxed
+    // accesses, not racing with the atomic adds of a render still running.
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < cells;
          i += gridDim.x * blockDim.x)
     {

@@ -141,6 +141,17 @@ constexpr int kHotSlotBits = 8;
 constexpr int kHotSlots = 1 << kHotSlotBits;
 constexpr int kHotCells = 64;
 constexpr unsigned int kHotEmpty = 0xFFFFFFFFu;
+// candidates a hot-cell search collects at most per threshold
+constexpr unsigned int kHotCollectCap = 1024;
+
+// Hot-cell table from candidate cells (count << 32 | cell, any order, from
+// launch_hot_collect) of a buffer holding about sum samples: the up to
+// kHotCells hottest, if together they hold at least 1/50 of sum, placed by
+// an odd multiplier under which no two share a slot.  On success *mult is
+// that multiplier, keys holds kHotSlots entries (kHotEmpty where unused)
+// and the result is true; found is sorted hottest first.
+bool hot_place(std::vector<unsigned long long>& found, unsigned long long sum,
+               unsigned int* mult, std::vector<unsigned int>& keys);
 
 // Dynamic shared memory of the plain and batch render kernels: the program,
 // ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), the
@@ -345,7 +356,9 @@ cudaError_t launch_hist_reduce(const unsigned int* counts, const unsigned int* h
                                cudaStream_t);
 
 // cells with count >= thr: out[0] = how many, out[1 ..] = (count << 32 |
-// cell) for the first cap of them (out holds 1 + cap words)
+// cell) for the first cap of them (out holds 1 + cap words).  Counts are
+// read with volatile (relaxed) loads, so a render may still be adding to
+// the buffer.
 cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, unsigned int thr,
                                unsigned long long* out, unsigned int cap, cudaStream_t);
 

@@ -77,6 +77,13 @@ struct SrvBuffer
     bool allocated = false;
     bool alloc_failed = false;
     std::vector<unsigned long long> init;   // -i data, added at admission
+    // hot-cell table of the render kernel (kHotSlots keys), searched once in
+    // the buffer's counts after its first finished round; hot_mult 0 = none
+    unsigned int* d_hot = nullptr;
+    unsigned int hot_mult = 0;
+    int hot_cells = 0;
+    bool hot_searched = false;
+    size_t smem_hot = 0;                // batch kernel shared memory with the table
     ~SrvBuffer();
     size_t file_bytes() const { return (size_t)flame.cells * (1 + (size_t)flame.color_dims) * 8; }
     size_t counts_bytes() const { return (size_t)flame.cells * 4; }
@@ -93,6 +100,7 @@ struct SrvJob
     DevStats* d_stats = nullptr;
     int slot = -1;                      // cancel flag index while admitted
     int spill = 0;
+    int hot_cells = 0;                  // hot-cell table cells of its last round
     int state = FFR_JOB_QUEUED;
     ffr_status status = FFR_OK;
     bool cancel_req = false;
@@ -152,6 +160,7 @@ struct Server
     std::condition_variable rd_cv;
     cudaEvent_t ev_alloc = nullptr;     // after the latest admission work
     unsigned long long* d_red = nullptr;    // 3 words: histogram sum, min, max
+    unsigned long long* d_hotc = nullptr;   // 1 + kHotCollectCap words: hot-cell search
     unsigned int* h_cancel = nullptr;   // mapped pinned flags, one per slot
     unsigned int* d_cancel = nullptr;
     std::vector<int> free_slots;
@@ -184,6 +193,7 @@ struct Server
     void admit_locked();
     bool launch_round_locked();
     void finish_round_locked(RoundSlot& r, cudaError_t e, const std::string& why);
+    void hot_search_locked(SrvBuffer& b, uint64_t sum);
     void finish_job_locked(SrvJob* j);
     void fail_job_locked(SrvJob* j, ffr_status st);
 };
@@ -197,6 +207,7 @@ SrvBuffer::~SrvBuffer()
     if (d_counts) cudaFreeAsync(d_counts, srv->aux);
     if (d_hi) cudaFreeAsync(d_hi, srv->aux);
     if (d_colors) cudaFreeAsync(d_colors, srv->aux);
+    if (d_hot) cudaFreeAsync(d_hot, srv->aux);
     srv->used.fetch_sub(dev_bytes);
 }
 
@@ -450,6 +461,18 @@ bool Server::launch_round_locked()
             jd.chunk_first = j->chunks_issued;
             groups[g].chunks += take[i];
             groups[g].smem = std::max(groups[g].smem, b.smem);
+            // the buffer's hot-cell table, while a chunk (kChunkStreams
+            // streams) stays below 2^32 samples (the table's u32 counts)
+            const uint64_t ntraj = (j->samples + j->L - 1) / j->L;
+            if (b.hot_mult && (long double)((ntraj + j->S - 1) / j->S) * j->L * kChunkStreams
+                                  < 4294967296.0L)
+            {
+                a.hot_keys = b.d_hot;
+                a.hot_mult = b.hot_mult;
+                a.agg = 0;
+                groups[g].smem = std::max(groups[g].smem, b.smem_hot);
+                j->hot_cells = b.hot_cells;
+            }
             groups[g].n += 1;
             j->chunks_issued += take[i];
             r->parts.push_back({j, take[i]});
@@ -604,6 +627,70 @@ void Server::finish_job_locked(SrvJob* j)
 }
 
 // Account a completed (or failed) round: chunks done, finished jobs.
+// Hot-cell table from a buffer holding about sum samples: candidates with at
+// least sum/4096 counts each (raising the threshold while more than
+// kHotCollectCap qualify), placed by hot_place.  Another round may still be
+// adding to the buffer; the collect kernel's relaxed loads see some of its
+// counts, which only moves the estimate.  Failures leave the buffer without
+// a table (renders do not need one).
+void Server::hot_search_locked(SrvBuffer& b, uint64_t sum)
+{
+    std::vector<unsigned long long> found;
+    cudaError_t e = cudaSuccess;
+    bool got = false;
+    uint64_t thr = std::max<uint64_t>(1, sum >> 12);
+    for (int it = 0; it < 12 && e == cudaSuccess && thr <= 0xFFFFFFFFull; ++it, thr *= 4)
+    {
+        unsigned long long n = 0;
+        e = launch_hot_collect(b.d_counts, (unsigned int)b.flame.cells, (unsigned int)thr, d_hotc,
+                               kHotCollectCap, aux);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&n, d_hotc, sizeof n, cudaMemcpyDeviceToHost, aux);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(aux);
+        if (e != cudaSuccess || n > kHotCollectCap)
+            continue;
+        found.resize(n);
+        if (n)
+        {
+            e = cudaMemcpyAsync(found.data(), d_hotc + 1, n * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, aux);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(aux);
+        }
+        got = e == cudaSuccess;
+        break;
+    }
+    unsigned int mult = 0;
+    std::vector<unsigned int> keys;
+    if (e != cudaSuccess)
+        cudaGetLastError();
+    if (!got || !hot_place(found, sum, &mult, keys))
+        return;
+    const size_t bytes = kHotSlots * sizeof(unsigned int);
+    e = pool_alloc(this, &b.d_hot, bytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b.d_hot, keys.data(), bytes, cudaMemcpyHostToDevice, aux);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(aux);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        if (b.d_hot)
+            cudaFreeAsync(b.d_hot, aux);
+        b.d_hot = nullptr;
+        return;
+    }
+    b.dev_bytes += bytes;
+    add_used(bytes);
+    b.hot_mult = mult;
+    b.hot_cells = (int)std::count_if(keys.begin(), keys.end(),
+                                     [](unsigned int k) { return k != kHotEmpty; });
+    b.smem_hot = chaos_smem_bytes<kChunkStreams>((unsigned int)b.prog.size(),
+                                                 (int)b.flame.xforms.size(),
+                                                 rsl_words_for(b.prog.data()), true);
+}
+
 void Server::finish_round_locked(RoundSlot& r, cudaError_t e, const std::string& why)
 {
     if (e != cudaSuccess)
@@ -613,6 +700,22 @@ void Server::finish_round_locked(RoundSlot& r, cudaError_t e, const std::string&
     }
     for (const RoundPart& p : r.parts)
         p.job->chunks_done += p.chunks;
+    // a buffer whose job has rounds to go gets its hot-cell table from the
+    // counts so far (once per buffer)
+    if (e == cudaSuccess)
+        for (const RoundPart& p : r.parts)
+        {
+            SrvJob* j = p.job;
+            SrvBuffer& b = *j->buf;
+            if (b.hot_searched || !b.allocated || j->state != FFR_JOB_RUNNING
+                || j->chunks_issued >= j->chunks_total || b.flame.cells >= (1ull << 30))
+                continue;
+            b.hot_searched = true;
+            const uint64_t sum = (uint64_t)((long double)j->samples * j->chunks_done
+                                            / j->chunks_total);
+            if (sum >= (1u << 16))
+                hot_search_locked(b, sum);
+        }
     for (const RoundPart& p : r.parts)
     {
         SrvJob* j = p.job;
@@ -923,8 +1026,10 @@ ffr_status ffr_server_create(const ffr_server_opts* opts, ffr_server** out)
         return cfail(e, "cudaEventCreate");
     if ((e = cudaEventRecord(s->ev_alloc, s->aux)) != cudaSuccess)
         return cfail(e, "cudaEventRecord");
-    if ((e = cudaMalloc(&s->d_red, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMalloc(&s->d_red, (4 + 1 + kHotCollectCap) * sizeof(unsigned long long)))
+            != cudaSuccess)
         return cfail(e, "cudaMalloc(reduction)");
+    s->d_hotc = s->d_red + 4;
     if ((e = cudaHostAlloc(&s->h_cancel, sizeof(unsigned int) * o.max_active,
                            cudaHostAllocMapped)) != cudaSuccess)
         return cfail(e, "cudaHostAlloc(cancel flags)");
@@ -1200,6 +1305,8 @@ ffr_status ffr_server_job_stats(ffr_server* srv, uint64_t job, ffr_stats* st)
     st->settle = s->o.settle;
     st->kernel_ms = j->t_done > j->t_submit ? (j->t_done - j->t_submit) * 1e-6 : 0.0;
     st->kernel = FFR_KERNEL_PLAIN;
+    st->agg = j->hot_cells ? 0 : kDefaultAgg;
+    st->hot_cells = j->hot_cells;
     return j->status;
 }
 

@@ -125,6 +125,31 @@ def test_continuation_adds_to_resident_buffer(ffr, flames):
             srv.release(j)
 
 
+def test_hot_cell_table_after_first_round(ffr, flames):
+    """A job of many rounds on a flame with hot cells counts them in shared
+    memory once its buffer's first round is in (the table comes from the
+    buffer's own counts); a continuation uses the table from its first
+    round.  Both equal their solo renders."""
+    text = json.dumps(flames.random_2d(7, size=(640, 360)))
+    cells = 640 * 360
+    with ffr.Server(precision=1, settle=SETTLE, round_chunks=16) as srv:
+        a = srv.submit(text, 40_000_000, 5)
+        assert srv.wait(a, 120_000).state == ffr.JOB_DONE
+        got_a = srv.read(a, cells)
+        st_a = srv.stats(a, 2)
+        b = srv.continue_(a, 20_000_000, 6)
+        assert srv.wait(b, 120_000).state == ffr.JOB_DONE
+        got_b = srv.read(b, cells)
+        st_b = srv.stats(b, 2)
+    want_a, ws_a, _ = solo(ffr, text, 40_000_000, 5, 1)
+    want_b, ws_b, _ = solo(ffr, text, 20_000_000, 6, 1)
+    assert st_a.hot_cells > 0 and st_b.hot_cells > 0
+    np.testing.assert_array_equal(got_a, want_a)
+    np.testing.assert_array_equal(got_b, want_a + want_b)
+    check_equal(got_a, want_a, st_a, ws_a)
+    assert st_b.samples_plotted == ws_b.samples_plotted
+
+
 def test_init_buffer_is_added(ffr, flames):
     """submit(init=...) adds a buffer file first (the reference's -i)."""
     text = golden_flame_text("color")
