@@ -285,6 +285,46 @@ ffr_status ensure_hi(ffr_ctx* c)
     return FFR_OK;
 }
 
+// Cancel flags: mapped pinned words handed out from per-device blocks of
+// kFlagBlock (pinning a page per context cost more than the rest of
+// ffr_create); a flag returns to its device's free list with its context.
+constexpr int kFlagBlock = 1024;
+std::mutex g_flag_mu;
+std::map<int, std::vector<std::pair<unsigned int*, unsigned int*>>> g_flag_free;
+
+cudaError_t take_flag(int device, unsigned int** h, unsigned int** d)
+{
+    std::lock_guard<std::mutex> lk(g_flag_mu);
+    auto& fl = g_flag_free[device];
+    if (fl.empty())
+    {
+        unsigned int* blk = nullptr;
+        unsigned int* dblk = nullptr;
+        cudaError_t e = cudaHostAlloc(&blk, kFlagBlock * sizeof(unsigned int),
+                                      cudaHostAllocMapped | cudaHostAllocPortable);
+        if (e != cudaSuccess)
+            return e;
+        if ((e = cudaHostGetDevicePointer(&dblk, blk, 0)) != cudaSuccess)
+        {
+            cudaFreeHost(blk);
+            return e;
+        }
+        for (int i = kFlagBlock - 1; i >= 0; --i)
+            fl.emplace_back(blk + i, dblk + i);
+    }
+    *h = fl.back().first;
+    *d = fl.back().second;
+    fl.pop_back();
+    *(volatile unsigned int*)*h = 0u;
+    return cudaSuccess;
+}
+
+void give_flag(int device, unsigned int* h, unsigned int* d)
+{
+    std::lock_guard<std::mutex> lk(g_flag_mu);
+    g_flag_free[device].emplace_back(h, d);
+}
+
 void destroy(ffr_ctx* c)
 {
     if (!c)
@@ -300,7 +340,7 @@ void destroy(ffr_ctx* c)
     cudaFree(c->d_scratch);
     cudaFree(c->d_hot);
     if (c->h_cancel)
-        cudaFreeHost(c->h_cancel);
+        give_flag(c->device, c->h_cancel, c->d_cancel);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->ev_done) cudaEventDestroy(c->ev_done);
@@ -872,11 +912,8 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
             || (e = cudaEventCreate(&c->ev1)) != cudaSuccess
             || (e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming)) != cudaSuccess)
         return cfail(e, "cudaEventCreate");
-    if ((e = cudaHostAlloc(&c->h_cancel, sizeof(unsigned int), cudaHostAllocMapped)) != cudaSuccess)
-        return cfail(e, "cudaHostAlloc");
-    *c->h_cancel = 0;
-    if ((e = cudaHostGetDevicePointer(&c->d_cancel, c->h_cancel, 0)) != cudaSuccess)
-        return cfail(e, "cudaHostGetDevicePointer");
+    if ((e = take_flag(c->device, &c->h_cancel, &c->d_cancel)) != cudaSuccess)
+        return cfail(e, "cudaHostAlloc(cancel flag)");
     // admission by free device memory
     const size_t need = c->flame.cells * sizeof(unsigned int)
         + c->flame.cells * (size_t)c->flame.color_dims * sizeof(double)
