@@ -348,7 +348,10 @@ def run_tetra3d(args):
     ffr, dev = got
     text = json.dumps(_flames().tetrahedron_3d((512, 512, 512)))
     B, settle = int(args.samples_per_step), 20
-    with ffr.BufferRenderer(text, precision=ffr.FP32, settle=settle, device=dev) as r:
+    kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
+            "hot": ffr.KERNEL_HOT}
+    with ffr.BufferRenderer(text, precision=ffr.FP32, settle=settle, device=dev,
+                            kernel=kern[args.kernel]) as r:
         sampler = ClockSampler(dev)
         sampler.start()
         # the 512 MiB buffer exceeds L2: no flush needed between steps

@@ -1119,6 +1119,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         ffr_status ts = ensure_hot_table(c, samples);
         if (ts != FFR_OK)
             return ts;
+        agg = agg_after_search(true);
     }
     uint64_t S = 0, L = 0;
     int grid = 0, kernel = 0;
@@ -1134,9 +1135,6 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     {
         a.hot_keys = c->d_hot;
         a.hot_mult = c->hot_mult;
-        // the table takes the collisions warp merging is for
-        if (c->opts.kernel == FFR_KERNEL_HOT)
-            a.agg = agg = 0;
     }
     *c->h_cancel = 0u;
     CU(c, cudaEventRecord(c->ev0, c->stream));
@@ -1688,7 +1686,8 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
                 return bfail(b, FFR_ERR_ARG, "too many samples per GPU thread (raise streams)");
             JobDesc& jd = g.h_jobs[k];
             fill_args(c, jd.a, N, seeds[g.members[k]], bad_limit, S, L, c->d_counts, c->d_hi,
-                      c->d_colors, c->d_stats, c->tuned ? c->tuned_agg : kDefaultAgg);
+                      c->d_colors, c->d_stats,
+                      c->tuned ? c->tuned_agg : agg_after_search(c->hot_searched));
             // the hot-cell table where the shared memory was sized for it and
             // a chunk (128 streams) stays below 2^32 samples (u32 counts)
             const int i = g.members[k];

@@ -59,18 +59,31 @@ __device__ __forceinline__ void load_program(unsigned char* dst, const unsigned 
         *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
 }
 
-// Affine::apply_to: ret = b; ret[i] += (0 + A[i][0] x[0] + ...)
+// Affine::apply_to: ret = b; ret[i] += (0 + A[i][0] x[0] + ...).  The
+// coefficients (A row-major kMaxDims x kMaxDims, then b; XformT keeps both
+// affines on 16-byte boundaries) come in 16-byte loads, the ones a
+// dimension does not use are never loaded.
 template <int D, typename R>
 __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
 {
+    constexpr int kN = kMaxDims * kMaxDims + kMaxDims;
+    constexpr int kPer = 16 / (int)sizeof(R);
+    static_assert(kN % kPer == 0, "affine coefficients fill whole 16-byte words");
+    R c[kN];
+#pragma unroll
+    for (int k = 0; k < kN; k += kPer)
+    {
+        const uint4 w = *reinterpret_cast<const uint4*>(aff + k);
+        memcpy(&c[k], &w, sizeof w);
+    }
 #pragma unroll
     for (int i = 0; i < D; ++i)
     {
         R d = R(0);
 #pragma unroll
         for (int j = 0; j < D; ++j)
-            d += aff[i * kMaxDims + j] * x[j];
-        out[i] = aff[kMaxDims * kMaxDims + i] + d;
+            d += c[i * kMaxDims + j] * x[j];
+        out[i] = c[kMaxDims * kMaxDims + i] + d;
     }
 }
 
@@ -150,10 +163,16 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
 // count instead of a search loop: lanes do not diverge on it.
 __device__ __forceinline__ int pick_branchless(const uint64_t* thresh, int nxf, uint64_t m)
 {
+    // thresholds in pairs (16-byte loads; the array is 16-byte aligned and
+    // holds nxf entries, so the pair of the last tested one is in bounds)
     int x = 0;
-#pragma unroll 4
-    for (int i = 0; i < nxf - 1; ++i)
-        x += m > thresh[i] ? 1 : 0;
+#pragma unroll 2
+    for (int i = 0; i < nxf - 1; i += 2)
+    {
+        const ulonglong2 t = *reinterpret_cast<const ulonglong2*>(thresh + i);
+        x += m > t.x ? 1 : 0;
+        x += (i + 1 < nxf - 1 && m > t.y) ? 1 : 0;
+    }
     return x;
 }
 

@@ -279,12 +279,17 @@ struct IsaacInit
     unsigned long long w[16];
 };
 
-// Warp-merged binning (RenderArgs::agg) where no autotuner decision exists:
-// lanes of a warp that hit the same cell make one atomic add.  Flames with
-// hot cells (fixed points, dense cores) gain much more (the 1920x1080
-// benchmark flame: 30 G binned/s merged, 22 unmerged) than flames without
-// collisions lose (a match per sample).
+// Warp-merged binning (RenderArgs::agg) where neither an autotuner decision
+// nor a hot-cell search exists: lanes of a warp that hit the same cell make
+// one atomic add.  Flames with hot cells (fixed points, dense cores) gain
+// much more (the 1920x1080 benchmark flame: 30 G binned/s merged, 22
+// unmerged) than flames without collisions lose (a match per sample).  Once
+// a search has run, flames with a hot-cell table count their hot cells in
+// shared memory and flames without one have no collisions worth merging
+// (a uniform Sierpinski triangle: 1.9 ms merged, 1.1 ms unmerged per 1e8
+// samples), so both bin unmerged (agg_after_search).
 constexpr int kDefaultAgg = 1;
+inline int agg_after_search(bool searched) { return searched ? 0 : kDefaultAgg; }
 
 // precision: 0 = FP64 mirror, 1 = FP32
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \

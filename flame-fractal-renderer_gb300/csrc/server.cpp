@@ -101,6 +101,7 @@ struct SrvJob
     int slot = -1;                      // cancel flag index while admitted
     int spill = 0;
     int hot_cells = 0;                  // hot-cell table cells of its last round
+    int last_agg = kDefaultAgg;         // warp merging of its last round
     int state = FFR_JOB_QUEUED;
     ffr_status status = FFR_OK;
     bool cancel_req = false;
@@ -452,7 +453,7 @@ bool Server::launch_round_locked()
             a.stats = j->d_stats;
             a.cancel = d_cancel + j->slot;
             a.rng_words = b.rng_words;
-            a.agg = kDefaultAgg;
+            a.agg = agg_after_search(b.hot_searched);
             a.rsl_words = rsl_words_for(b.prog.data());
             std::memcpy(a.isaac_init, isaac_init, sizeof a.isaac_init);
             set_geometry(a, b.prog.data(), o.precision);
@@ -473,6 +474,7 @@ bool Server::launch_round_locked()
                 groups[g].smem = std::max(groups[g].smem, b.smem_hot);
                 j->hot_cells = b.hot_cells;
             }
+            j->last_agg = a.agg;
             groups[g].n += 1;
             j->chunks_issued += take[i];
             r->parts.push_back({j, take[i]});
@@ -1305,7 +1307,7 @@ ffr_status ffr_server_job_stats(ffr_server* srv, uint64_t job, ffr_stats* st)
     st->settle = s->o.settle;
     st->kernel_ms = j->t_done > j->t_submit ? (j->t_done - j->t_submit) * 1e-6 : 0.0;
     st->kernel = FFR_KERNEL_PLAIN;
-    st->agg = j->hot_cells ? 0 : kDefaultAgg;
+    st->agg = j->last_agg;
     st->hot_cells = j->hot_cells;
     return j->status;
 }
