@@ -33,6 +33,38 @@ def test_library_exports_every_declared_symbol(ffr):
     assert exported == set(header_functions())
 
 
+# the ctypes mirrors of the header's structs, field by field
+STRUCTS = {"ffr_opts": "Opts", "ffr_stats": "Stats", "ffr_image_info": "ImageInfo",
+           "ffr_server_opts": "ServerOpts", "ffr_job_info": "JobInfo"}
+
+
+def test_struct_layouts_match_ctypes(ffr, tmp_path):
+    """sizeof and every field offset of the header's structs, compiled by
+    the C compiler, against the ctypes classes the binding uses."""
+    lines = []
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(ffr, pyname)
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in cls._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "ffr_gpu.h"\n'
+                   "int main(void) {\n" + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src),
+                           "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    import ctypes
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(ffr, pyname)
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for field, _ in cls._fields_:
+            assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
+
+
 @pytest.mark.parametrize("name", sorted(MAN["invalid"]))
 def test_invalid_flames_rejected_through_abi(ffr, name):
     case = MAN["invalid"][name]
