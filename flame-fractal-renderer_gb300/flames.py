@@ -48,6 +48,18 @@ def sierpinski_2d(size=(1024, 1024)) -> dict:
             "xforms": xfs}
 
 
+def heavy_point_2d(size=(640, 360)) -> dict:
+    """Three contractions by 1/2 with weights 0.9 / 0.05 / 0.05: the measure
+    piles up at the heavy map's fixed point, so a few cells hold most samples
+    (a flame for the hot-cell table).  Linear maps only: FP64 renders are
+    bit-exact against the oracle."""
+    def xf(w, bx, by):
+        return {"weight": w, "variations": [{"name": "linear", "weight": 1.0}],
+                "pre_affine": {"A": [[0.5, 0.0], [0.0, 0.5]], "b": [bx, by]}}
+    return {"dimensions": 2, "size": list(size), "bounds": [[-1.0, 1.0], [-1.0, 1.0]],
+            "xforms": [xf(0.9, 0.13, 0.21), xf(0.05, -0.5, 0.4), xf(0.05, 0.45, -0.5)]}
+
+
 def tetrahedron_3d(size=(512, 512, 512)) -> dict:
     verts = [(1, 1, 1), (1, -1, -1), (-1, 1, -1), (-1, -1, 1)]
     xfs = []

@@ -16,15 +16,8 @@ PLAIN, HOT = 1, 3
 
 
 def heavy_point_flame(size=(640, 360)):
-    """Three contractions by 1/2 with weights 0.9 / 0.05 / 0.05: the measure
-    piles up at the heavy map's fixed point (a few cells hold most samples).
-    Linear maps only, so FP64 renders are bit-exact against the oracle."""
-    def xf(w, bx, by):
-        return {"weight": w, "variations": [{"name": "linear", "weight": 1.0}],
-                "pre_affine": {"A": [[0.5, 0.0], [0.0, 0.5]], "b": [bx, by]}}
-    return {"dimensions": 2, "size": list(size),
-            "bounds": [[-1.0, 1.0], [-1.0, 1.0]],
-            "xforms": [xf(0.9, 0.13, 0.21), xf(0.05, -0.5, 0.4), xf(0.05, 0.45, -0.5)]}
+    import flames
+    return flames.heavy_point_2d(size)
 
 
 def render_pair(ffr, text, precision, samples, seed, S, L, preload=None):
