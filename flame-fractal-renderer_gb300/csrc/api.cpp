@@ -589,26 +589,10 @@ ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long*
     if (sum < 4096)
         return FFR_OK;
     std::vector<unsigned long long> found;
-    for (uint64_t thr = sum >> 12; thr <= red[2]; thr *= 4)
-    {
-        CU(c, launch_hot_collect(counts, (unsigned int)cells,
-                                 (unsigned int)std::min<uint64_t>(thr, 0xFFFFFFFFull), out,
-                                 kHotCollectCap, c->stream));
-        unsigned long long n = 0;
-        CU(c, cudaMemcpyAsync(&n, out, sizeof n, cudaMemcpyDeviceToHost, c->stream));
-        CU(c, cudaStreamSynchronize(c->stream));
-        if (n > kHotCollectCap)
-            continue;           // too many at this threshold: raise it
-        found.resize(n);
-        if (n)
-        {
-            CU(c, cudaMemcpyAsync(found.data(), out + 1, n * sizeof(unsigned long long),
-                                  cudaMemcpyDeviceToHost, c->stream));
-            CU(c, cudaStreamSynchronize(c->stream));
-        }
-        break;
-    }
-    if (!hot_place(found, sum, mult, keys))
+    bool got = false;
+    CU(c, collect_hot_candidates(counts, (unsigned int)cells, sum >> 12, red[2], out, c->stream,
+                                 found, &got));
+    if (!got || !hot_place(found, sum, mult, keys))
         *mult = 0;
     return FFR_OK;
 }

@@ -320,6 +320,43 @@ cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, u
     return cudaGetLastError();
 }
 
+cudaError_t collect_hot_candidates(const unsigned int* counts, unsigned int cells,
+                                   unsigned long long thr, unsigned long long thr_max,
+                                   unsigned long long* out, cudaStream_t st,
+                                   std::vector<unsigned long long>& found, bool* got)
+{
+    *got = false;
+    found.clear();
+    thr = thr ? thr : 1;
+    for (; thr <= thr_max && thr <= 0xFFFFFFFFull; thr *= 4)
+    {
+        unsigned long long n = 0;
+        cudaError_t e = launch_hot_collect(counts, cells, (unsigned int)thr, out, kHotCollectCap,
+                                           st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&n, out, sizeof n, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            return e;
+        if (n > kHotCollectCap)
+            continue;           // too many at this threshold: raise it
+        found.resize(n);
+        if (n)
+        {
+            e = cudaMemcpyAsync(found.data(), out + 1, n * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess)
+                return e;
+        }
+        *got = true;
+        return cudaSuccess;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_hist_reduce(const unsigned int* counts, const unsigned int* hi,
                                unsigned long long cells, unsigned long long* out,
                                cudaStream_t st)

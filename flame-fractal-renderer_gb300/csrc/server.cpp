@@ -638,31 +638,9 @@ void Server::finish_job_locked(SrvJob* j)
 void Server::hot_search_locked(SrvBuffer& b, uint64_t sum)
 {
     std::vector<unsigned long long> found;
-    cudaError_t e = cudaSuccess;
     bool got = false;
-    uint64_t thr = std::max<uint64_t>(1, sum >> 12);
-    for (int it = 0; it < 12 && e == cudaSuccess && thr <= 0xFFFFFFFFull; ++it, thr *= 4)
-    {
-        unsigned long long n = 0;
-        e = launch_hot_collect(b.d_counts, (unsigned int)b.flame.cells, (unsigned int)thr, d_hotc,
-                               kHotCollectCap, aux);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&n, d_hotc, sizeof n, cudaMemcpyDeviceToHost, aux);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(aux);
-        if (e != cudaSuccess || n > kHotCollectCap)
-            continue;
-        found.resize(n);
-        if (n)
-        {
-            e = cudaMemcpyAsync(found.data(), d_hotc + 1, n * sizeof(unsigned long long),
-                                cudaMemcpyDeviceToHost, aux);
-            if (e == cudaSuccess)
-                e = cudaStreamSynchronize(aux);
-        }
-        got = e == cudaSuccess;
-        break;
-    }
+    cudaError_t e = collect_hot_candidates(b.d_counts, (unsigned int)b.flame.cells, sum >> 12,
+                                           0xFFFFFFFFull, d_hotc, aux, found, &got);
     unsigned int mult = 0;
     std::vector<unsigned int> keys;
     if (e != cudaSuccess)
