@@ -632,7 +632,6 @@ ffr_status ensure_hot_table(ffr_ctx* c, uint64_t samples)
     const size_t need = off_hs + (1 + kHotCollectCap) * sizeof(unsigned long long);
     unsigned char* buf = nullptr;
     CU(c, cudaMalloc(&buf, need));
-    CU(c, cudaMemsetAsync(buf, 0, c->flame.cells * 4, c->stream));
     unsigned int* pc = reinterpret_cast<unsigned int*>(buf);
     DevStats* pst = reinterpret_cast<DevStats*>(buf + off_st);
     double* pcol = r ? reinterpret_cast<double*>(buf + off_col) : nullptr;
@@ -641,7 +640,14 @@ ffr_status ensure_hot_table(ffr_ctx* c, uint64_t samples)
         samples, c->opts.precision == FFR_FP64 ? (1u << 22) : (1u << 24)));
     uint64_t S = 0, L = 0;
     int grid = 0, kk = 0;
-    ffr_status st = plan(c, P, FFR_KERNEL_PLAIN, &S, &L, &grid, &kk);
+    ffr_status st = FFR_OK;
+    {
+        cudaError_t e = cudaMemsetAsync(buf, 0, c->flame.cells * 4, c->stream);
+        if (e != cudaSuccess)
+            st = cuda_fail(c, e, "hot-cell probe");
+    }
+    if (st == FFR_OK)
+        st = plan(c, P, FFR_KERNEL_PLAIN, &S, &L, &grid, &kk);
     if (st == FFR_OK)
         st = reset_stats(c, pst);
     if (st == FFR_OK)
@@ -740,6 +746,13 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     float best = 1e30f;
     int best_k = *kernel, best_a = 0;
     bool best_h = false;
+    ffr_status st = FFR_OK;
+    {
+        // the probes' counts locate the hot cells: start them from zero
+        cudaError_t e = cudaMemsetAsync(pc, 0, cells * 4, c->stream);
+        if (e != cudaSuccess)
+            st = cuda_fail(c, e, "autotune scratch");
+    }
     // one candidate: time two probe launches, keep the faster candidate
     auto probe = [&](int k, int g, bool h) -> ffr_status {
         uint64_t S = 0, L = 0;
@@ -776,7 +789,6 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         }
         return FFR_OK;
     };
-    ffr_status st = FFR_OK;
     for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED})
         for (int g : {0, 1})
             if (st == FFR_OK)
