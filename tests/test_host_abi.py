@@ -152,6 +152,16 @@ def test_flame_generators_are_seeded(flames):
 
 def test_generated_flames_parse_in_oracle(fo, flames):
     for fl in (flames.sierpinski_2d(), flames.tetrahedron_3d(), flames.random_2d(7),
-               flames.random_3d(5)):
+               flames.random_3d(5), flames.heavy_point_2d()):
         f = fo.load_flame(json.dumps(fl))
         assert abs(sum(x.weight for x in f.xforms) / sum(x.weight for x in f.xforms) - 1) == 0
+
+
+def test_heavy_point_flame_concentrates(fo, flames):
+    """The hot-cell test flame (oracle, CPU): its 64 hottest cells hold most
+    of the samples, far above the 1/50 a hot-cell table needs."""
+    import numpy as np
+    of = fo.OracleFlame(fo.load_flame(json.dumps(flames.heavy_point_2d((64, 64)))))
+    r = fo.render(of, 1, 256, 200_000, 500, 20)
+    c = np.sort(r.counts)[::-1]
+    assert c[:64].sum() > 0.9 * c.sum()
