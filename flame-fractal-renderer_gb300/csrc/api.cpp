@@ -174,7 +174,7 @@ struct ffr_ctx
     int tuned_kernel = FFR_KERNEL_PLAIN;
     int tuned_agg = 0;
     bool tuned_hot = false;
-    bool hot_searched = false;      // FFR_KERNEL_HOT's probe has run
+    bool hot_searched = false;      // a hot-cell search ran (probe or autotuner)
     // hot-cell table of the plain kernel (kHotSlots keys), installed by the
     // autotuner; hot_mult 0 = none
     unsigned int* d_hot = nullptr;
@@ -710,6 +710,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
             c->tuned_kernel = *kernel = ch.kernel;
             c->tuned_agg = *agg = ch.agg;
             c->tuned_hot = *hot = ch.hot_mult != 0;
+            c->hot_searched = true;
             return FFR_OK;
         }
     }
@@ -818,6 +819,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     c->tuned_kernel = *kernel = best_k;
     c->tuned_agg = *agg = best_a;
     c->tuned_hot = *hot = best_h;
+    // the table (or its absence) is the autotuner's decision: batches reuse it
+    c->hot_searched = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     if (g_tune_cache.size() > 4096)
         g_tune_cache.clear();
