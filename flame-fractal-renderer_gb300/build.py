@@ -83,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
-    for name in ("api", "server", "png", "flame", "json", "variations_host"):
+    for name in ("api", "server", "png", "flame", "json", "variations_host", "hot_cells"):
         src = os.path.join(CSRC, name + ".cpp")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [*cxx_common, "-c", src, "-o", obj]))
