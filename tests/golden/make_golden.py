@@ -140,6 +140,7 @@ RENDERS = [
     ("ties", 15, 8, 20000, 1000, 20, 256, "mirror"),
     ("badval", 17, 8, 20000, 1000, 20, 1000000000, "mirror"),
     ("julia3", 19, 8, 20000, 1000, 20, 256, "mirror"),
+    ("heavy", 23, 64, 200000, 500, 20, 256, "mirror"),
 ]
 
 # parameters for every variation that takes any (keys as the reference reads them)
@@ -296,6 +297,9 @@ def main():
     os.makedirs(DATA, exist_ok=True)
     allf = dict(FLAME_SET)
     allf.update(edge_flames())
+    # a density piled up at one fixed point (the kernels' hot-cell table);
+    # last, so the seeded inputs of the flames above stay as they were
+    allf["heavy"] = gen.heavy_point_2d(size=(64, 64))
     manifest = {"kat": {}, "flames": {}, "renders": [], "invalid": {}, "valid_edge": {}}
     # KATs
     kat = {}

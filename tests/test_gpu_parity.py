@@ -22,7 +22,7 @@ from conftest import GOLDEN, golden_flame_text, golden_manifest
 pytestmark = pytest.mark.gpu
 
 MAN = golden_manifest()
-ALGEBRAIC = {"sierpinski", "tetra", "alg2d", "color", "ties", "badval"}
+ALGEBRAIC = {"sierpinski", "tetra", "alg2d", "color", "ties", "badval", "heavy"}
 STEP_REL = 1e-12
 
 
