@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libffr_gpu.so")
 CLI_PATH = os.path.join(HERE, "_build", "ffr-buf")
 
-FFR_ABI_VERSION = 1
+FFR_ABI_VERSION = 2
 MAX_DIMS = 3
 MAX_XFORM_IDS = 4096
 MAX_BAD_RECORDS = 4096

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FFR_ABI_VERSION 1
+#define FFR_ABI_VERSION 2
 
 typedef enum ffr_status {
     FFR_OK = 0,

@@ -94,6 +94,32 @@ def test_default_opts(ffr):
     assert o.settle == 53 and o.precision == ffr.FP64 and o.streams == 0
 
 
+def test_abi_version_matches_header(ffr):
+    text = open(os.path.join(ROOT, "include", "ffr_gpu.h")).read()
+    m = re.search(r"#define FFR_ABI_VERSION (\d+)", text)
+    assert m and int(m.group(1)) == ffr.FFR_ABI_VERSION
+
+
+def test_kernel_option_range(ffr):
+    """ffr_create accepts FFR_KERNEL_AUTO..FFR_KERNEL_HOT and rejects other
+    values before any device work (so this runs without a GPU)."""
+    import ctypes
+    lib = ffr.load_library()
+    raw = json.dumps({"dimensions": 1, "size": [8], "bounds": [[-1, 1]],
+                      "xforms": [{"weight": 1, "variations": [{"name": "linear",
+                                                               "weight": 1}]}]}).encode()
+    for kernel, rejected in ((-1, True), (4, True), (ffr.KERNEL_HOT, False)):
+        o = ffr.Opts()
+        lib.ffr_default_opts(ctypes.byref(o))
+        o.kernel = kernel
+        ctx = ctypes.c_void_p()
+        st = lib.ffr_create(raw, len(raw), ctypes.byref(o), ctypes.byref(ctx))
+        msg = lib.ffr_last_error(None).decode()
+        if st == ffr.FFR_OK:
+            lib.ffr_destroy(ctx)
+        assert (st == ffr.FFR_ERR_ARG and "kernel" in msg) == rejected, (kernel, st, msg)
+
+
 def test_isaac_words_rejects_null(ffr):
     lib = ffr.load_library()
     assert lib.ffr_isaac_words(0, 1, 4, None) == ffr.FFR_ERR_ARG
