@@ -15,7 +15,8 @@ value   device time of the render kernel (CUDA events on the library's
         writing a 256 MiB buffer (the buffer itself, 8.3 MB, fits in L2)
 e2e     the same metric through the C ABI with host buffers: every step
         creates the context from the JSON text (parse + program upload),
-        renders, and reads the buffer back into pinned host memory
+        renders, reads the buffer back into pinned host memory (allocated
+        once, before timing) and destroys the context
 roofline  binned samples x 8 B (one 4-byte atomic read-modify-write each)
         against measured HBM bandwidth, plus the measured rate of 4-byte
         atomic adds at random cells of a buffer of the same size (l2_atomic)
@@ -27,6 +28,9 @@ tv      FP32 against FP64 at a fixed sample count: total-variation distance
         beside the FP64 seed-to-seed noise floor at the same count
 
 --impl reference times that CPU implementation alone, as the reference arm.
+--kernel auto|plain|sorted|hot picks the render kernel (default: the
+library's autotuner; hot = the plain kernel with the flame's hottest cells
+counted in shared memory) for the default and tetra3d workloads.
 
 Other configurations (--workload; each prints its own JSON line):
   sierpinski  2-D Sierpinski triangle, 1024x1024, 1e8 samples from 1e6
