@@ -30,7 +30,7 @@ tv      FP32 against FP64 at a fixed sample count: total-variation distance
 --impl reference times that CPU implementation alone, as the reference arm.
 --kernel auto|plain|sorted|hot picks the render kernel (default: the
 library's autotuner; hot = the plain kernel with the flame's hottest cells
-counted in shared memory) for the default and tetra3d workloads.
+counted in shared memory) for the default, sierpinski and tetra3d workloads.
 
 Other configurations (--workload; each prints its own JSON line):
   sierpinski  2-D Sierpinski triangle, 1024x1024, 1e8 samples from 1e6
