@@ -276,13 +276,13 @@ def _line(args, workload, value, ms_per_step, dtype, config, **extra):
 
 def _timed_steps(r, args, samples, seed0, flush=None):
     """args.warmup untimed renders, then args.steps timed ones; returns
-    (kernel ms, binned, iterated, last stats)."""
+    (kernel ms, binned, iterated, last stats, kernels launched while timed)."""
     import torch
     for w in range(args.warmup):
         r.render(samples, seed0 + 10_000 + w, bad_limit=10**12)
     r.clear()
     ms = 0.0
-    binned = iters = 0
+    binned = iters = launches = 0
     s = None
     for k in range(args.steps):
         if flush is not None:
@@ -292,7 +292,10 @@ def _timed_steps(r, args, samples, seed0, flush=None):
         ms += s.kernel_ms
         binned += s.samples_plotted - s.dropped
         iters += s.samples_iterated
-    return ms, binned, iters, s
+        # the render kernel plus the library's own extra launches (count-bound
+        # reductions between accumulating steps)
+        launches += 1 + s.aux_launches
+    return ms, binned, iters, s, launches
 
 
 def run_sierpinski(args):
@@ -307,6 +310,7 @@ def run_sierpinski(args):
     N, T, Lt, settle = 10**8, 10**6, 100, 20
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
     res = {}
+    launches = 0
     sampler = ClockSampler(dev)
     sampler.start()
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
@@ -314,7 +318,8 @@ def run_sierpinski(args):
     for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
         with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
                                 device=dev, kernel=kern[args.kernel]) as r:
-            ms, binned, iters, s = _timed_steps(r, args, N, 1, flush)
+            ms, binned, iters, s, n_launch = _timed_steps(r, args, N, 1, flush)
+            launches += n_launch
             res[name] = {"value": binned / (ms * 1e-3), "ms_per_step": ms / args.steps,
                          "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel)}
             if name == "fp64" and args.verify:
@@ -337,7 +342,7 @@ def run_sierpinski(args):
           v, res["fp64"]["ms_per_step"], "f64",
           {"samples_per_step": N, "trajectories": T, "traj_len": Lt, "settle": settle,
            "seed": 1, "flush": "256 MiB L2 flush between timed steps"},
-          fp32=res["fp32"], gpu_launches=args.steps * 2,
+          fp32=res["fp32"], gpu_launches=launches,
           l2_atomic={"peak_ops_per_s": atom, "frac_fp64": v / atom,
                      "frac_fp32": res["fp32"]["value"] / atom},
           verify=verify, clocks=clocks)
@@ -359,7 +364,7 @@ def run_tetra3d(args):
         sampler = ClockSampler(dev)
         sampler.start()
         # the 512 MiB buffer exceeds L2: no flush needed between steps
-        ms, binned, iters, s = _timed_steps(r, args, B, 3)
+        ms, binned, iters, s, launches = _timed_steps(r, args, B, 3)
         clocks = sampler.stop()
         assert r.histogram()[0] == binned
         import numpy as np
@@ -378,7 +383,7 @@ def run_tetra3d(args):
           {"samples_per_step": B, "settle": settle, "seed": 3, "streams": s.streams,
            "traj_len": s.traj_len, "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel),
            "flush": "none: the 512 MiB buffer is larger than L2"},
-          gpu_launches=args.steps,
+          gpu_launches=launches,
           roofline={"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
                     "peak_source": kind},
@@ -411,13 +416,14 @@ def run_batch256(args):
             r.clear()
         sampler = ClockSampler(dev)
         sampler.start()
-        ms, binned = 0.0, 0
+        ms, binned, aux = 0.0, 0, 0
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             _, sts = b.render(ns, [1000 * k + i for i in range(len(ns))], bad_limit=10**12)
             ms += sts[0].kernel_ms
             binned += sum(st.samples_plotted - st.dropped for st in sts)
+            aux += sum(st.aux_launches for st in sts)
         clocks = sampler.stop()
         nhot = sum(1 for st in sts if st.hot_cells)
     for r in rs:
@@ -435,7 +441,7 @@ def run_batch256(args):
            "traj_len": 4096, "kernel": "persistent batch (CUDA graph)",
            "hot_cell_tables": f"{nhot} of {len(texts)} jobs",
            "flush": "256 MiB L2 flush between timed steps"},
-          gpu_launches=args.steps * 2,
+          gpu_launches=args.steps * 2 + aux,
           tv={"per_flame": tvs,
               "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
           clocks=clocks)
@@ -666,7 +672,7 @@ def main():
         kern_ms += s.kernel_ms
         binned += s.samples_plotted - s.dropped
         iters += s.samples_iterated
-        launches += 1
+        launches += 1 + s.aux_launches
         streams, traj_len = s.streams, s.traj_len
         kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel) + (
             " + warp-merged bins" if s.agg else "") + (

@@ -132,6 +132,8 @@ struct ffr_ctx
     unsigned int* d_hot = nullptr;
     unsigned int hot_mult = 0;
     int hot_cells = 0;
+    // kernels launched by the current call besides the render kernel
+    unsigned int aux_launches = 0;
     std::string err = "no error";
 
     const Launchers& L() const { return kLaunchers[opts.precision][flame.dims - 1]; }
@@ -535,6 +537,7 @@ ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long*
     unsigned long long init[3] = {0ull, ~0ull, 0ull}, red[3];
     CU(c, cudaMemcpyAsync(out, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
     CU(c, launch_hist_reduce(counts, nullptr, cells, out, c->stream));
+    ++c->aux_launches;
     CU(c, cudaMemcpyAsync(red, out, sizeof red, cudaMemcpyDeviceToHost, c->stream));
     CU(c, cudaStreamSynchronize(c->stream));
     const uint64_t sum = red[0];
@@ -543,7 +546,7 @@ ffr_status hot_table(ffr_ctx* c, const unsigned int* counts, unsigned long long*
     std::vector<unsigned long long> found;
     bool got = false;
     CU(c, collect_hot_candidates(counts, (unsigned int)cells, sum >> 12, red[2], out, c->stream,
-                                 found, &got));
+                                 found, &got, &c->aux_launches));
     if (!got || !hot_place(found, sum, mult, keys))
         *mult = 0;
     return FFR_OK;
@@ -609,6 +612,8 @@ ffr_status ensure_hot_table(ffr_ctx* c, uint64_t samples)
         cudaError_t e = c->L().render(a, grid, c->stream);
         if (e != cudaSuccess)
             st = cuda_fail(c, e, "hot-cell probe");
+        else
+            ++c->aux_launches;
     }
     unsigned int mult = 0;
     std::vector<unsigned int> keys;
@@ -729,6 +734,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
             CU(c, cudaEventRecord(c->ev0, c->stream));
             CU(c, kk == FFR_KERNEL_SORTED ? c->L().sorted(a, grid, c->stream)
                                           : c->L().render(a, grid, c->stream));
+            ++c->aux_launches;
             CU(c, cudaEventRecord(c->ev1, c->stream));
             CU(c, cudaEventSynchronize(c->ev1));
             CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -1043,6 +1049,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->xform_ids = c->flame.xform_ids;
         st->settle = c->opts.settle;
     }
+    c->aux_launches = 0;
     if (samples == 0)
         return FFR_OK;      // render(0) returns true (buffer_renderer.hpp:276-277)
     CU(c, cudaSetDevice(c->device));
@@ -1112,6 +1119,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->kernel = kernel;
         st->agg = agg;
         st->hot_cells = hot ? c->hot_cells : 0;
+        st->aux_launches = (int32_t)c->aux_launches;
     }
     if (hs.cancelled)
         return fail(c, FFR_ERR_TIMEOUT, "render cancelled");
@@ -1149,6 +1157,7 @@ ffr_status ffr_histogram(ffr_ctx* c, uint64_t* sum, uint64_t* mn, uint64_t* mx)
     unsigned long long* d = c->d_scratch + (c->scratch_bytes / 8 - 4);
     CU(c, cudaMemcpyAsync(d, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
     CU(c, launch_hist_reduce(c->d_counts, c->d_hi, c->flame.cells, d, c->stream));
+    ++c->aux_launches;
     CU(c, cudaMemcpyAsync(out, d, sizeof out, cudaMemcpyDeviceToHost, c->stream));
     s = wait_stream(c);
     if (s != FFR_OK)
@@ -1603,6 +1612,8 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
     const size_t n = b->ctxs.size();
     b->job_hot.assign(n, 0);
     b->job_agg.assign(n, 0);
+    for (size_t i = 0; i < n; ++i)
+        b->ctxs[i]->aux_launches = 0;
     // streams and trajectory length per job, high-word planes where needed
     for (size_t i = 0; i < n; ++i)
     {
@@ -1712,6 +1723,7 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
         st->kernel = FFR_KERNEL_PLAIN;
         st->agg = b->job_agg[i];
         st->hot_cells = b->job_hot[i];
+        st->aux_launches = (int32_t)c->aux_launches;
     }
     return worst;
 }

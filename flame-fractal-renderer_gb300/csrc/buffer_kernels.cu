@@ -323,7 +323,8 @@ cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, u
 cudaError_t collect_hot_candidates(const unsigned int* counts, unsigned int cells,
                                    unsigned long long thr, unsigned long long thr_max,
                                    unsigned long long* out, cudaStream_t st,
-                                   std::vector<unsigned long long>& found, bool* got)
+                                   std::vector<unsigned long long>& found, bool* got,
+                                   unsigned int* launches)
 {
     *got = false;
     found.clear();
@@ -333,6 +334,8 @@ cudaError_t collect_hot_candidates(const unsigned int* counts, unsigned int cell
         unsigned long long n = 0;
         cudaError_t e = launch_hot_collect(counts, cells, (unsigned int)thr, out, kHotCollectCap,
                                            st);
+        if (e == cudaSuccess && launches)
+            ++*launches;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(&n, out, sizeof n, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess)

@@ -369,11 +369,13 @@ cudaError_t launch_hot_collect(const unsigned int* counts, unsigned int cells, u
 // Hot-cell candidates into found (host): cells with count >= thr, the
 // threshold raised fourfold while more than kHotCollectCap qualify (up to
 // thr_max); *got is false when no threshold left few enough.  out: 1 +
-// kHotCollectCap device words; waits for the stream.
+// kHotCollectCap device words; waits for the stream.  *launches (or null)
+// grows by the kernels launched.
 cudaError_t collect_hot_candidates(const unsigned int* counts, unsigned int cells,
                                    unsigned long long thr, unsigned long long thr_max,
                                    unsigned long long* out, cudaStream_t st,
-                                   std::vector<unsigned long long>& found, bool* got);
+                                   std::vector<unsigned long long>& found, bool* got,
+                                   unsigned int* launches);
 
 cudaError_t launch_atomic_rate(unsigned int* buf, unsigned int cells, unsigned int iters,
                                int grid, int block, unsigned int salt, cudaStream_t);

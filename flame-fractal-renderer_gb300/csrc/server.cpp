@@ -640,7 +640,7 @@ void Server::hot_search_locked(SrvBuffer& b, uint64_t sum)
     std::vector<unsigned long long> found;
     bool got = false;
     cudaError_t e = collect_hot_candidates(b.d_counts, (unsigned int)b.flame.cells, sum >> 12,
-                                           0xFFFFFFFFull, d_hotc, aux, found, &got);
+                                           0xFFFFFFFFull, d_hotc, aux, found, &got, nullptr);
     unsigned int mult = 0;
     std::vector<unsigned int> keys;
     if (e != cudaSuccess)

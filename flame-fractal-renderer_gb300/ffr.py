@@ -82,7 +82,7 @@ class Stats(ctypes.Structure):
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
                 ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32),
-                ("hot_cells", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("hot_cells", ctypes.c_int32), ("aux_launches", ctypes.c_int32)]
 
 
 class ImageInfo(ctypes.Structure):
@@ -215,6 +215,7 @@ class RenderStats:
     kernel: int
     agg: int
     hot_cells: int = 0
+    aux_launches: int = 0
 
     @property
     def ok(self) -> bool:
@@ -232,7 +233,8 @@ def _render_stats(status: int, st: Stats, n: int) -> RenderStats:
         bad_xf=np.array(st.bad_xf[:nrec], dtype=np.uint64),
         bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
         streams=st.streams, traj_len=st.traj_len, settle=st.settle,
-        kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg, hot_cells=st.hot_cells)
+        kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg, hot_cells=st.hot_cells,
+        aux_launches=st.aux_launches)
 
 
 def isaac_words(key: int, n: int, device: int = 0) -> np.ndarray:
@@ -441,7 +443,7 @@ class Batch:
                 bad_xf=np.array(st.bad_xf[:st.bad_recorded], dtype=np.uint64),
                 bad_pts=np.zeros((0, d)), streams=st.streams, traj_len=st.traj_len,
                 settle=st.settle, kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg,
-                hot_cells=st.hot_cells))
+                hot_cells=st.hot_cells, aux_launches=st.aux_launches))
         return status, out
 
     def close(self):

@@ -113,7 +113,9 @@ typedef struct ffr_stats {
     int32_t agg;                 /* 1: equal-cell increments were warp-merged */
     int32_t hot_cells;           /* cells counted in per-CTA shared memory
                                     (the autotuner's hot-cell table), or 0 */
-    int32_t reserved;
+    int32_t aux_launches;        /* kernels this call launched besides the
+                                    render kernel: count-bound reductions,
+                                    autotuner probes, hot-cell search */
 } ffr_stats;
 
 typedef struct ffr_ctx ffr_ctx;

@@ -227,8 +227,10 @@ def test_many_renders_into_one_buffer(ffr, flames):
     text = json.dumps(flames.random_2d(7, size=(640, 360)))
     parts = [(2_000_000_000, 31), (2_000_000_000, 32), (1_000_000_000, 33)]
     with ffr.BufferRenderer(text, precision=1, settle=20, traj_len=4096) as r:
-        for n, seed in parts:
-            r.render(n, seed, bad_limit=10**12)
+        sts = [r.render(n, seed, bad_limit=10**12) for n, seed in parts]
+        # the second render stays under the running bound; the third passes it
+        # and launches one reduction for the exact largest count
+        assert sts[1].aux_launches == 0 and sts[2].aux_launches == 1
         got = r.counts()
         total = sum(n for n, _ in parts)
         want = np.zeros_like(got)
