@@ -1,14 +1,21 @@
 // Instantiates the chaos kernels for one (precision, dims) pair; compiled
 // once per pair and kind with -DFFR_P=<0|1> -DFFR_D=<1|2|3>
-// -DFFR_KIND=<0|1> (0: plain render, step and trace kernels; 1: the
-// xform-sorted render kernel), so the objects compile in parallel.  The FP64 objects are
+// -DFFR_KIND=<0..5>, so the objects compile in parallel:
+//   0  plain render kernel without colour (and the colour dispatch)
+//   1  xform-sorted render kernel
+//   2  plain render kernel with colour
+//   3  persistent batch kernel without colour (and the colour dispatch)
+//   4  persistent batch kernel with colour
+//   5  single-step and trace kernels
+// Each render kernel inlines every variation, so one kernel per object keeps
+// the slowest object (FP64 without contraction) short.  The FP64 objects are
 // built with --fmad=false so no multiply-add is contracted: the reference
 // (and the oracle) round every product and sum separately.
 #include "chaos_kernel.cuh"
 #include "chaos_sorted.cuh"
 
 #if !defined(FFR_P) || !defined(FFR_D) || !defined(FFR_KIND)
-#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3> -DFFR_KIND=<0|1>"
+#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3> -DFFR_KIND=<0..5>"
 #endif
 
 #define FFR_CAT2(a, b, c, d) a##_p##b##_d##c##d
@@ -23,9 +30,17 @@ using Real = double;
 using Real = float;
 #endif
 
-#if FFR_KIND == 0
+// the colour instantiations live in their own objects (kinds 2 and 4)
+cudaError_t FFR_NAME(launch_render_color)(const RenderArgs& a, int grid, cudaStream_t st);
+cudaError_t FFR_NAME(occupancy_color)(int rsl_words, int hot, int* blocks_per_sm,
+                                      unsigned int prog_bytes, int nxf, size_t* smem);
+cudaError_t FFR_NAME(launch_batch_color)(const BatchArgs& b, int grid, size_t smem,
+                                         cudaStream_t st);
+cudaError_t FFR_NAME(occupancy_batch_color)(int* blocks_per_sm, size_t smem);
 
 constexpr int kBlock = 128;
+
+#if FFR_KIND == 0 || FFR_KIND == 2
 
 template <bool C>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
@@ -55,18 +70,38 @@ static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_w
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, kBlock, smem);
 }
 
+#endif
+
+#if FFR_KIND == 0
+
 cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t st)
 {
-    return a.color_dims > 0 ? launch_one<true>(a, grid, st) : launch_one<false>(a, grid, st);
+    return a.color_dims > 0 ? FFR_NAME(launch_render_color)(a, grid, st)
+                            : launch_one<false>(a, grid, st);
 }
 
 cudaError_t FFR_NAME(occupancy)(int color, int rsl_words, int hot, int* blocks_per_sm,
                                 int* block, unsigned int prog_bytes, int nxf, size_t* smem)
 {
     *block = kBlock;
-    return color ? occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
+    return color ? FFR_NAME(occupancy_color)(rsl_words, hot, blocks_per_sm, prog_bytes, nxf, smem)
                  : occ_one<false>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
 }
+
+#elif FFR_KIND == 2
+
+cudaError_t FFR_NAME(launch_render_color)(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    return launch_one<true>(a, grid, st);
+}
+
+cudaError_t FFR_NAME(occupancy_color)(int rsl_words, int hot, int* blocks_per_sm,
+                                      unsigned int prog_bytes, int nxf, size_t* smem)
+{
+    return occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
+}
+
+#elif FFR_KIND == 3 || FFR_KIND == 4
 
 template <bool C>
 static cudaError_t batch_attr(size_t smem)
@@ -75,27 +110,55 @@ static cudaError_t batch_attr(size_t smem)
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+template <bool C>
+static cudaError_t batch_launch(const BatchArgs& b, int grid, size_t smem, cudaStream_t st)
+{
+    chaos_batch_kernel<FFR_D, Real, C, kBlock><<<grid, kBlock, smem, st>>>(b);
+    return cudaGetLastError();
+}
+
+template <bool C>
+static cudaError_t batch_occ(int* blocks_per_sm, size_t smem)
+{
+    cudaError_t e = batch_attr<C>(smem);
+    if (e != cudaSuccess)
+        return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        blocks_per_sm, chaos_batch_kernel<FFR_D, Real, C, kBlock>, kBlock, smem);
+}
+
+#if FFR_KIND == 3
+
 cudaError_t FFR_NAME(launch_batch)(const BatchArgs& b, int color, int grid, size_t smem,
                                    cudaStream_t st)
 {
-    if (color)
-        chaos_batch_kernel<FFR_D, Real, true, kBlock><<<grid, kBlock, smem, st>>>(b);
-    else
-        chaos_batch_kernel<FFR_D, Real, false, kBlock><<<grid, kBlock, smem, st>>>(b);
-    return cudaGetLastError();
+    return color ? FFR_NAME(launch_batch_color)(b, grid, smem, st)
+                 : batch_launch<false>(b, grid, smem, st);
 }
 
 cudaError_t FFR_NAME(occupancy_batch)(int color, int* blocks_per_sm, int* block, size_t smem)
 {
     *block = kBlock;
-    cudaError_t e = color ? batch_attr<true>(smem) : batch_attr<false>(smem);
-    if (e != cudaSuccess)
-        return e;
-    return color ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                       blocks_per_sm, chaos_batch_kernel<FFR_D, Real, true, kBlock>, kBlock, smem)
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                       blocks_per_sm, chaos_batch_kernel<FFR_D, Real, false, kBlock>, kBlock, smem);
+    return color ? FFR_NAME(occupancy_batch_color)(blocks_per_sm, smem)
+                 : batch_occ<false>(blocks_per_sm, smem);
 }
+
+#else
+
+cudaError_t FFR_NAME(launch_batch_color)(const BatchArgs& b, int grid, size_t smem,
+                                         cudaStream_t st)
+{
+    return batch_launch<true>(b, grid, smem, st);
+}
+
+cudaError_t FFR_NAME(occupancy_batch_color)(int* blocks_per_sm, size_t smem)
+{
+    return batch_occ<true>(blocks_per_sm, smem);
+}
+
+#endif
+
+#elif FFR_KIND == 5
 
 cudaError_t FFR_NAME(launch_step)(const StepArgs& a, cudaStream_t st)
 {
@@ -126,7 +189,7 @@ cudaError_t FFR_NAME(launch_trace)(const TraceArgs& a, cudaStream_t st)
     return cudaGetLastError();
 }
 
-#else
+#elif FFR_KIND == 1
 
 constexpr int kSortedBlock = 256;
 

@@ -7,9 +7,20 @@
 //
 // GPU meaning of the reference's work-split options:
 //   -b/--batch-size  samples per trajectory (the reference starts a new
-//                    trajectory per batch, buffer_renderer.hpp:155); 0 picks
-//                    samples / streams so every GPU thread has one trajectory
-//   -t/--threads     accepted and echoed; the device decides its parallelism
+//                    trajectory per batch, buffer_renderer.hpp:155).  0 is
+//                    the reference's automatic size, clamp((samples + 255)
+//                    >> 8, 4096, 2^20) (ffr_buf.cpp:94-101), so the same
+//                    command restarts and settles trajectories as often as
+//                    the reference does; with --streams, 0 instead picks
+//                    samples / streams (one trajectory per GPU thread).
+//                    Below 256 is rejected when rendering, as render() does
+//                    (buffer_renderer.hpp:283-285).
+//   -t/--threads     checked as render() checks it (1..65535,
+//                    buffer_renderer.hpp:277-282) and echoed; the device
+//                    decides its parallelism
+// The render-time checks of -t and -b run before the flame is read (the
+// reference runs them when render() starts, after reading the flame and the
+// input buffers), so a command with a bad flame and a bad -t reports -t.
 // Added options: --seed N (stream seeds; default from the clock, like the
 // reference's per-thread clock seeding), --precision fp64|fp32, --settle N
 // (default 53 = settle_iters<double>), --streams N, --trajectories T (T
@@ -207,12 +218,27 @@ int main(int argc, char** argv)
         die("the option '--flame' is required but missing");
     if (!a.have_output)
         die("the option '--output' is required but missing");
+    const bool user_batch = a.batch != 0;
     if (a.trajectories)
     {
         if (a.batch || a.streams)
             die("--trajectories excludes --batch-size and --streams");
         a.streams = a.trajectories;
         a.batch = a.samples ? (a.samples + a.trajectories - 1) / a.trajectories : 1;
+    }
+    // the reference's automatic batch size (ffr_buf.cpp:94-101)
+    const bool calculated_batch = a.batch == 0 && a.streams == 0;
+    if (calculated_batch)
+        a.batch = std::clamp<uint64_t>((a.samples + 255) >> 8, 1u << 12, 1u << 20);
+    // BufferRenderer::render's argument checks (buffer_renderer.hpp:277-285)
+    if (a.samples > 0)
+    {
+        if (a.threads == 0)
+            die("BufferRenderer::render(): threads must be positive");
+        if (a.threads > 65535)
+            die("BufferRenderer::render(): too many threads");
+        if (user_batch && a.batch < 256)
+            die("BufferRenderer::render(): batch size too small");
     }
     if (!a.have_seed)
         a.seed = (uint64_t)std::chrono::steady_clock::now().time_since_epoch().count()
@@ -229,6 +255,17 @@ int main(int argc, char** argv)
         std::cerr << " (not rendering)";
     std::cerr << std::endl;
     std::cerr << "--threads " << a.threads << std::endl;
+    // a batch size known without the device is echoed where the reference
+    // echoes it, before the flame is read (ffr_buf.cpp:115-118)
+    const bool batch_known = a.batch != 0;
+    if (batch_known)
+    {
+        if (calculated_batch)
+            std::cerr << "--batch_size 0 (" << a.batch << ")" << std::endl;
+        else
+            std::cerr << "--batch_size " << a.batch << std::endl;
+        std::cerr << "--bad_values " << a.bad_values << std::endl;
+    }
 
     std::string text;
     if (a.flame == "-")
@@ -255,11 +292,12 @@ int main(int argc, char** argv)
     uint64_t streams = 0, traj_len = a.batch;
     if (a.samples)
         check(ctx, ffr_plan(ctx, a.samples, &streams, &traj_len));
-    if (a.batch == 0)
+    if (!batch_known)
+    {
+        // --streams with -b 0: the trajectory length comes from the plan
         std::cerr << "--batch_size 0 (" << traj_len << ")" << std::endl;
-    else
-        std::cerr << "--batch_size " << a.batch << std::endl;
-    std::cerr << "--bad_values " << a.bad_values << std::endl;
+        std::cerr << "--bad_values " << a.bad_values << std::endl;
+    }
     std::cerr << "--seed " << a.seed << std::endl;
     std::cerr << "--precision " << (a.precision == FFR_FP64 ? "fp64" : "fp32") << std::endl;
     std::cerr << "--settle " << a.settle << std::endl;

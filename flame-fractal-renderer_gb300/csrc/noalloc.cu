@@ -17,6 +17,7 @@
 #include "ffr_gpu.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -91,6 +92,24 @@ ffr_status scratch_for(int device, unsigned char** out)
     return FFR_OK;
 }
 
+// a caller buffer must be device (or managed) memory of the render's device:
+// the kernel dereferences it there
+ffr_status device_buffer(const void* p, int device, const char* name)
+{
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nocuda(e, (std::string("ffr_render_noalloc: ") + name).c_str());
+    }
+    if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+            || (at.type == cudaMemoryTypeDevice && at.device != device))
+        return nofail(FFR_ERR_ARG, std::string("ffr_render_noalloc: ") + name
+            + " is not device memory of device " + std::to_string(device));
+    return FFR_OK;
+}
+
 void pick_launchers(int precision, int dims, RenderFn* r, OccFn* o)
 {
     static const RenderFn rf[2][3] = {
@@ -124,6 +143,15 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     if (o.abi_version != FFR_ABI_VERSION
             || (o.precision != FFR_FP64 && o.precision != FFR_FP32))
         return nofail(FFR_ERR_ARG, "ffr_render_noalloc: bad options");
+    // the autotuner, the xform-sorted kernel and the hot-cell search all need
+    // device memory of their own, and a bounded wait needs a mapped cancel
+    // flag: this entry point runs the plain kernel and waits until it ends
+    if (o.kernel != FFR_KERNEL_AUTO && o.kernel != FFR_KERNEL_PLAIN)
+        return nofail(FFR_ERR_ARG, "ffr_render_noalloc: only the plain kernel runs here "
+                                   "(opts.kernel must be FFR_KERNEL_AUTO or FFR_KERNEL_PLAIN)");
+    if (o.timeout_ms != 0)
+        return nofail(FFR_ERR_ARG, "ffr_render_noalloc: no bounded wait here "
+                                   "(opts.timeout_ms must be 0)");
     if (samples > 0xFFFFFFFFull)
         return nofail(FFR_ERR_ARG, "ffr_render_noalloc: at most 2^32-1 samples per call "
                                    "(u32 cells, no high-word buffer)");
@@ -161,8 +189,13 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     if (samples == 0)
         return FFR_OK;
     cudaError_t e;
+    ffr_status s0;
     if ((e = cudaSetDevice(o.device)) != cudaSuccess)
         return nocuda(e, "cudaSetDevice");
+    if ((s0 = device_buffer(d_counts, o.device, "d_counts")) != FFR_OK)
+        return s0;
+    if (f.color_dims > 0 && (s0 = device_buffer(d_colors, o.device, "d_colors")) != FFR_OK)
+        return s0;
     unsigned char* scratch = nullptr;
     ffr_status s = scratch_for(o.device, &scratch);
     if (s != FFR_OK)
@@ -233,10 +266,13 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     a.rsl_words = rsl_words_for(prog.data());
     isaac_init_table(a.isaac_init);
     set_geometry(a, prog.data(), o.precision);
+    const auto t0 = std::chrono::steady_clock::now();
     if ((e = render(a, (int)blocks, st)) != cudaSuccess)
         return nocuda(e, "render launch");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
         return nocuda(e, "render");
+    const double wall_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if ((e = cudaMemcpy(&head, dstats, sizeof head, cudaMemcpyDeviceToHost)) != cudaSuccess)
         return nocuda(e, "cudaMemcpy(stats)");
     if (stats)
@@ -247,11 +283,17 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
             return nocuda(e, "cudaMemcpy(stats)");
         const unsigned long long nrec =
             head.bad_claim < (unsigned long long)kMaxBadRecords ? head.bad_claim : kMaxBadRecords;
+        // the kernel writes a record's first dims coordinates only: the
+        // others hold whatever an earlier call on this device left there
+        std::vector<double> pts(kMaxDims * nrec);
         if (nrec && ((e = cudaMemcpy(stats->bad_xf, dstats->bad_xf, 8 * nrec,
                                      cudaMemcpyDeviceToHost)) != cudaSuccess
-                     || (e = cudaMemcpy(stats->bad_pts, dstats->bad_pts, 8 * kMaxDims * nrec,
+                     || (e = cudaMemcpy(pts.data(), dstats->bad_pts, 8 * kMaxDims * nrec,
                                         cudaMemcpyDeviceToHost)) != cudaSuccess))
             return nocuda(e, "cudaMemcpy(stats)");
+        for (unsigned long long k = 0; k < nrec; ++k)
+            for (int i = 0; i < f.dims; ++i)
+                stats->bad_pts[k][i] = pts[k * kMaxDims + i];
         stats->samples_iterated = head.s_iter;
         stats->samples_plotted = head.s_plot;
         stats->bad_values = head.bad_total;
@@ -267,6 +309,8 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
         stats->bad_recorded = nrec;
         stats->streams = S;
         stats->traj_len = L;
+        stats->kernel = FFR_KERNEL_PLAIN;
+        stats->kernel_ms = wall_ms;
     }
     if (head.stop)
         return nofail(FFR_BAD_VALUES, "render failure (flame may not be sufficiently contractive)");

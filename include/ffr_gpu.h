@@ -411,7 +411,15 @@ ffr_status ffr_measure_atomic_rate(int device, uint64_t cells, uint64_t ops,
  * that device current); make that first call before any stream capture.
  * Calls share the array: calls that overlap on the GPU (from several host
  * threads) race, so serialise them.  Work runs on the legacy default stream
- * and the call returns when it is done.  Errors: ffr_last_error(NULL).
+ * and the call returns when it is done.
+ * Options: precision, device, settle, streams and traj_len as in
+ * ffr_render; kernel must be FFR_KERNEL_AUTO or FFR_KERNEL_PLAIN (the plain
+ * kernel always runs: the tuner, the xform-sorted kernel and the hot-cell
+ * search would need device memory) and timeout_ms must be 0 (the call waits
+ * for the kernel to end), else FFR_ERR_ARG.  d_counts (and d_colors for a
+ * colour flame) must be memory of opts->device, else FFR_ERR_ARG.
+ * stats->kernel_ms is the host wall time from launch to completion.
+ * Errors: ffr_last_error(NULL).
  * ------------------------------------------------------------------- */
 ffr_status ffr_render_noalloc(const char *json, size_t len, const ffr_opts *opts,
                               uint32_t *d_counts, double *d_colors, uint64_t cells,

@@ -164,6 +164,52 @@ def test_cli_rejects_bad_flame(ffr, tmp_path):
     assert b"ERROR:" in r.stderr and b"low >= high" in r.stderr
 
 
+@pytest.mark.parametrize("args,msg", [
+    (["-s", "1000", "-t", "0"], b"BufferRenderer::render(): threads must be positive"),
+    (["-s", "1000", "-t", "65536"], b"BufferRenderer::render(): too many threads"),
+    (["-s", "1000", "-b", "255"], b"BufferRenderer::render(): batch size too small"),
+    (["-s", "1000", "-b", "1"], b"BufferRenderer::render(): batch size too small"),
+])
+def test_cli_render_argument_checks(ffr, tmp_path, args, msg):
+    """render()'s checks of threads and batch size (buffer_renderer.hpp:277-285),
+    made before any device work."""
+    r = run_cli(ffr, ["-f", str(tmp_path / "none.json"), "-o", str(tmp_path / "o.buf"), *args])
+    assert r.returncode == 1 and msg in r.stderr, r.stderr
+
+
+def test_cli_render_argument_checks_need_samples(ffr, tmp_path):
+    """With no samples render() returns before its checks: -t 0 and -b 1 pass
+    and the command fails only at the missing flame file."""
+    r = run_cli(ffr, ["-f", str(tmp_path / "none.json"), "-o", str(tmp_path / "o.buf"),
+                      "-t", "0", "-b", "1"])
+    assert r.returncode == 1 and b"BufferRenderer" not in r.stderr
+    assert b"cannot open flame file" in r.stderr
+
+
+@pytest.mark.parametrize("samples,batch", [(1000, 4096), (10**7, 39063), (10**12, 1 << 20),
+                                           (0, 4096)])
+def test_cli_automatic_batch_size(ffr, tmp_path, samples, batch):
+    """-b 0 is the reference's clamp((N + 255) >> 8, 4096, 2^20)
+    (ffr_buf.cpp:94-101), echoed before the flame is read."""
+    r = run_cli(ffr, ["-f", str(tmp_path / "none.json"), "-o", str(tmp_path / "o.buf"),
+                      "-s", str(samples), "-t", "4"])
+    assert f"--batch_size 0 ({batch})\n".encode() in r.stderr, r.stderr
+    lines = r.stderr.decode().splitlines()
+    assert lines.index("--threads 4") + 1 == lines.index(f"--batch_size 0 ({batch})")
+
+
+def test_cli_explicit_batch_and_trajectories_echo(ffr, tmp_path):
+    base = ["-f", str(tmp_path / "none.json"), "-o", str(tmp_path / "o.buf"), "-s", "100000"]
+    r = run_cli(ffr, base + ["-b", "300"])
+    assert b"--batch_size 300\n" in r.stderr
+    # --trajectories: N samples from T trajectories may mean fewer than 256
+    # samples each (the project's extension; no batch check applies)
+    r = run_cli(ffr, base + ["--trajectories", "1000"])
+    assert b"--batch_size 100\n" in r.stderr and b"too small" not in r.stderr
+    r = run_cli(ffr, base + ["--trajectories", "10", "-b", "300"])
+    assert r.returncode == 1 and b"excludes" in r.stderr
+
+
 def test_flame_generators_are_seeded(flames):
     a = json.dumps(flames.random_2d(7))
     b = json.dumps(flames.random_2d(7))

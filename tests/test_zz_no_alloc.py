@@ -49,9 +49,10 @@ def test_noalloc_matches_ffr_render_two_calls(ffr, flames):
     buf = torch.zeros(cells, dtype=torch.int32, device="cuda:0")     # caller-owned
     torch.cuda.synchronize()
     o = _opts(ffr, settle, streams, traj_len)
+    plotted = 0
     with ffr.BufferRenderer(text, precision=ffr.FP64, settle=settle, streams=streams,
                             traj_len=traj_len) as r:
-        for k, seed in enumerate((11, 12)):
+        for seed in (11, 12):
             st = _noalloc(ffr, text, ctypes.c_void_p(buf.data_ptr()), None, cells, n, seed, o)
             ref = r.render(n, seed)              # accumulates like the caller's buffer
             got = buf.cpu().numpy().view(np.uint32).astype(np.uint64)
@@ -61,7 +62,86 @@ def test_noalloc_matches_ffr_render_two_calls(ffr, flames):
             assert [st.xf_dist[i] for i in range(3)] == ref.xf_dist.tolist()
             assert [st.ext_lo[i] for i in range(2)] == ref.ext_lo.tolist()
             assert [st.ext_hi[i] for i in range(2)] == ref.ext_hi.tolist()
-            assert got.sum() == (k + 1) * n or got.sum() == r.histogram()[0]
+            assert st.kernel == 1                # FFR_KERNEL_PLAIN
+            # the caller's buffer holds every sample both calls binned
+            plotted += st.samples_plotted
+            assert int(got.sum()) == plotted
+
+
+def test_noalloc_allocates_no_device_memory(ffr, flames):
+    """The defining property: after a first call (which looks up the scratch
+    array and loads the kernel), further calls leave the device's free memory
+    exactly where it was."""
+    torch = pytest.importorskip("torch")
+    text = json.dumps(flames.sierpinski_2d(size=(128, 128)))
+    buf = torch.zeros(128 * 128, dtype=torch.int32, device="cuda:0")
+    torch.cuda.synchronize()
+    o = _opts(ffr, 20, 1024, 500)
+    ptr = ctypes.c_void_p(buf.data_ptr())
+    _noalloc(ffr, text, ptr, None, 128 * 128, 500_000, 1, o)
+    free0, _ = torch.cuda.mem_get_info(0)
+    for seed in (2, 3, 4):
+        _noalloc(ffr, text, ptr, None, 128 * 128, 500_000, seed, o)
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+
+
+def _expanding(dims, size):
+    """Every xform triples the point: trajectories leave 1e20 within 45
+    steps, so a render records many bad values."""
+    eye = [[3.0 if i == j else 0.0 for j in range(dims)] for i in range(dims)]
+    return json.dumps({"dimensions": dims, "size": [size] * dims,
+                       "bounds": [[-1.0, 1.0]] * dims,
+                       "xforms": [{"weight": 1.0, "variations": [{"name": "linear", "weight": 1.0}],
+                                   "pre_affine": {"A": eye, "b": [0.1] * dims}}]})
+
+
+def test_noalloc_bad_value_records_only_the_flames_dims(ffr):
+    """Bad-value records of a 2-D call after a 3-D one: the scratch array keeps
+    the 3-D call's coordinates, the 2-D call reports only its own two."""
+    torch = pytest.importorskip("torch")
+    lib = ffr.load_library()
+    o = _opts(ffr, 20, 256, 400)
+    for dims, size in ((3, 16), (2, 64)):
+        text = _expanding(dims, size)
+        cells = size ** dims
+        buf = torch.zeros(cells, dtype=torch.int32, device="cuda:0")
+        torch.cuda.synchronize()
+        st = ffr.Stats()
+        raw = text.encode()
+        rc = lib.ffr_render_noalloc(raw, len(raw), ctypes.byref(o),
+                                    ctypes.c_void_p(buf.data_ptr()), None, cells, 100_000, 7,
+                                    10**9, ctypes.byref(st))
+        assert rc == ffr.FFR_OK, lib.ffr_last_error(None).decode()
+        n = st.bad_recorded
+        assert n > 100 and st.bad_values >= n
+        pts = np.array([[st.bad_pts[k][i] for i in range(3)] for k in range(n)])
+        big = ~(np.abs(pts[:, :dims]) <= 1e20)       # beyond the threshold, or NaN
+        assert big.any(axis=1).all()
+        if dims == 2:
+            assert (pts[:, 2] == 0.0).all()
+
+
+def test_noalloc_rejects_options_it_cannot_honour(ffr, flames):
+    torch = pytest.importorskip("torch")
+    lib = ffr.load_library()
+    raw = json.dumps(flames.sierpinski_2d(size=(8, 8))).encode()
+    owned = torch.zeros(64, dtype=torch.int32, device="cuda:0")
+    torch.cuda.synchronize()
+    ptr = ctypes.c_void_p(owned.data_ptr())
+    for field, value in (("kernel", 2), ("kernel", 3), ("timeout_ms", 100)):
+        o = _opts(ffr, 20, 0, 0)
+        setattr(o, field, value)
+        rc = lib.ffr_render_noalloc(raw, len(raw), ctypes.byref(o), ptr, None, 64, 1000, 1,
+                                    256, None)
+        assert rc == ffr.FFR_ERR_ARG, field
+    # host memory is not the device's: refused before any launch
+    host = np.zeros(64, dtype=np.uint32)
+    rc = lib.ffr_render_noalloc(raw, len(raw), ctypes.byref(_opts(ffr, 20, 0, 0)),
+                                host.ctypes.data_as(ctypes.c_void_p), None, 64, 1000, 1, 256,
+                                None)
+    assert rc == ffr.FFR_ERR_ARG and b"device memory" in lib.ffr_last_error(None)
+    assert (host == 0).all()
 
 
 def test_noalloc_colour_flame(ffr):
