@@ -17,11 +17,21 @@ e2e     the same metric through the C ABI with host buffers: every step
         creates the context from the JSON text (parse + program upload),
         renders, reads the buffer back into pinned host memory (allocated
         once, before timing) and destroys the context
-roofline  binned samples x 8 B (one 4-byte atomic read-modify-write each)
-        against measured HBM bandwidth, plus the measured rate of 4-byte
-        atomic adds at random cells of a buffer of the same size (l2_atomic)
+roofline  bound "l2_atomic": binned samples per launch (one 4-byte atomic
+        add each) over the launch's event time, against the rate of 4-byte
+        atomic adds at uniformly random cells of a buffer of the same size
+        measured in the same run; roofline_hbm: the same adds as 8 B of
+        read-modify-write against the measured HBM copy bandwidth
 cpu_baseline  the oracle's C restatement of the reference path (FP64,
-        all host threads) on a bounded sample of the same workload
+        all host threads) on a bounded sample of the same workload, with
+        its measured speed against the reference's own render()
+        (port_vs_reference, oracle/port_vs_reference.py)
+batch256  the 256-flame batch in one persistent graph launch (2 timed
+        steps, per-flame TV of 8 flames against FP64)
+serving  the Poisson request stream twice: at 200 req/s (over capacity;
+        its served rate is the capacity) and at 0.7x that capacity, each
+        with p50/p99 latency and its own clock record; latency_ms at the
+        top level is the sustainable stream's
 
 tv      FP32 against FP64 at a fixed sample count: total-variation distance
         between the FP32 histogram and an FP64 (reference arithmetic) one,
@@ -62,6 +72,12 @@ sys.path.insert(0, os.path.join(ROOT, "flame-fractal-renderer_gb300"))
 import __graft_entry__ as ge  # noqa: E402
 
 METRIC = "binned samples/s"
+# the oracle port against the reference's own BufferRenderer::render() on the
+# same flame and host (oracle/port_vs_reference.py, FP64, settle 53, the
+# reference's automatic batch size; x86-64, 8 cores): the reference sources,
+# and so oracle/_ref, exist only where the reference was checked out
+PORT_VS_REFERENCE = {"threads_8": 3.47, "threads_4": 2.54, "threads_1": 1.07,
+                     "host": "x86-64, 8 cores", "script": "oracle/port_vs_reference.py"}
 WORKLOAD = "random 2-D flame, 6 xforms x 2 variations, 1920x1080, 1e10 samples"
 
 
@@ -218,7 +234,8 @@ def run_reference(args):
                    "seed": 7, "flush": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"{args.steps} x {per} samples of the workload, FP64"},
+                         "sample": f"{args.steps} x {per} samples of the workload, FP64",
+                         "port_vs_reference": PORT_VS_REFERENCE},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "iterated_per_s": iters / dt,
@@ -394,12 +411,11 @@ def run_tetra3d(args):
           tv=tv, clocks=clocks, iterated_per_s=iters / (ms * 1e-3))
 
 
-def run_batch256(args):
-    """256 random 2-D flames in one persistent, graph-captured launch per step."""
-    got = _setup_single(args)
-    if got is None:
-        return
-    ffr, dev = got
+def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8):
+    """The 256-flame batch (flames.batch_jobs(11)) in one persistent,
+    graph-captured launch per step: binned samples/s over `steps` timed
+    steps (L2 flushed between them), per-flame TV against FP64 for n_tv
+    flames, and the clocks seen while timing."""
     import torch
     fl = _flames()
     jobs = fl.batch_jobs(11)
@@ -409,55 +425,70 @@ def run_batch256(args):
           for t in texts]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
     with ffr.Batch(rs) as b:
-        for w in range(args.warmup):
+        for w in range(warmup):
             b.render([max(1, n // 100) for n in ns], [500 + i for i in range(len(ns))],
                      bad_limit=10**12, stats=False)
         for r in rs:
             r.clear()
         sampler = ClockSampler(dev)
         sampler.start()
-        ms, binned, aux = 0.0, 0, 0
-        for k in range(args.steps):
+        ms, binned, iters, aux = 0.0, 0, 0, 0
+        for k in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             _, sts = b.render(ns, [1000 * k + i for i in range(len(ns))], bad_limit=10**12)
             ms += sts[0].kernel_ms
             binned += sum(st.samples_plotted - st.dropped for st in sts)
+            iters += sum(st.samples_iterated for st in sts)
             aux += sum(st.aux_launches for st in sts)
         clocks = sampler.stop()
         nhot = sum(1 for st in sts if st.hot_cells)
     for r in rs:
         r.close()
-    value = binned / (ms * 1e-3)
     tvs = []
-    if not args.no_tv:
-        for i in range(0, len(texts), len(texts) // 8):
+    if with_tv:
+        for i in range(0, len(texts), len(texts) // n_tv):
             t = tv_check(ffr, texts[i], 10**8, 20, dev)
             t["flame"] = i
             tvs.append(t)
-    _line(args, "256 random 2-D flames (2-8 xforms, 256^2-2048^2, 1e7-1e9 samples) "
-          "in one persistent launch", value, ms / args.steps, "f32",
-          {"flames": len(texts), "samples_per_step": sum(ns), "settle": 20, "seed": 11,
-           "traj_len": 4096, "kernel": "persistent batch (CUDA graph)",
-           "hot_cell_tables": f"{nhot} of {len(texts)} jobs",
-           "flush": "256 MiB L2 flush between timed steps"},
-          gpu_launches=args.steps * 2 + aux,
-          tv={"per_flame": tvs,
-              "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
-          clocks=clocks)
+    return {"value": binned / (ms * 1e-3), "unit": "samples/s", "ms_per_step": ms / steps,
+            "steps": steps, "warmup": warmup, "iterated_per_s": iters / (ms * 1e-3),
+            "flames": len(texts), "samples_per_step": sum(ns), "settle": 20, "seed": 11,
+            "traj_len": 4096, "kernel": "persistent batch (CUDA graph)",
+            "hot_cell_tables": f"{nhot} of {len(texts)} jobs",
+            "flush": "256 MiB L2 flush between timed steps",
+            "gpu_launches": steps * 2 + aux,
+            "tv": {"per_flame": tvs,
+                   "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
+            "clocks": clocks}
 
 
-def run_serving(args):
-    """Poisson request stream through the serving loop (ffr_server_*)."""
+def run_batch256(args):
+    """256 random 2-D flames in one persistent, graph-captured launch per step."""
     got = _setup_single(args)
     if got is None:
         return
     ffr, dev = got
+    rec = batch256_record(ffr, dev, args.steps, args.warmup, with_tv=not args.no_tv)
+    _line(args, "256 random 2-D flames (2-8 xforms, 256^2-2048^2, 1e7-1e9 samples) "
+          "in one persistent launch", rec["value"], rec["ms_per_step"], "f32",
+          {k: rec[k] for k in ("flames", "samples_per_step", "settle", "seed", "traj_len",
+                               "kernel", "hot_cell_tables", "flush")},
+          gpu_launches=rec["gpu_launches"], tv=rec["tv"], clocks=rec["clocks"],
+          iterated_per_s=rec["iterated_per_s"])
+
+
+def serving_record(ffr, dev, rate, duration, warmup, max_active, with_tv=True, n_tv=4):
+    """A Poisson request stream (flames.serving_requests(23, rate, duration))
+    through the serving loop (ffr_server_*), every result read back by four
+    client threads: binned samples/s from the first submission to the last
+    completion, p50/p99 latency (submission to completion, and with the
+    read-back), and TV against FP64 for n_tv served 2-D jobs."""
     import queue
     import random
     import numpy as np
     fl = _flames()
-    reqs = fl.serving_requests(23, args.rate, args.duration)
+    reqs = fl.serving_requests(23, rate, duration)
     texts = [json.dumps(f) if f is not None else None for _, _, f, _ in reqs]
     geo = []
     for _, kind, f, _ in reqs:
@@ -469,9 +500,9 @@ def run_serving(args):
                 cells *= x
             geo.append((cells, f["dimensions"]))
     srv = ffr.Server(precision=ffr.FP32, settle=20, traj_len=4096, device=dev,
-                     max_active=args.max_active)
+                     max_active=max_active)
     # warm-up: a few small jobs of each kind (module load, pool growth)
-    for w in range(max(1, args.warmup)):
+    for w in range(max(1, warmup)):
         a = srv.submit(texts[0], 10**6, 9000 + w)
         srv.wait(a, 60_000)
         srv.release(a)
@@ -560,7 +591,7 @@ def run_serving(args):
     first = min(r[1] for r in results)
     last = max(r[2] for r in results)
     span = (last - first) * 1e-9
-    offered = sum(n for *_, n in reqs) / args.duration
+    offered = sum(n for *_, n in reqs) / duration
     kinds = {}
     for r in results:
         kinds.setdefault(r[0], []).append((r[2] - r[1]) * 1e-6)
@@ -568,8 +599,8 @@ def run_serving(args):
     # solo FP32 render with streams = ceil(N / 4096) (tests/test_gpu_server.py),
     # so four 2-D requests of at most 2e8 samples are re-rendered that way
     tvs = []
-    if not args.no_tv:
-        picks = [i for i, (_, k, _, n) in enumerate(reqs) if k == "2d" and n <= 2 * 10**8][:4]
+    if with_tv:
+        picks = [i for i, (_, k, _, n) in enumerate(reqs) if k == "2d" and n <= 2 * 10**8][:n_tv]
         for i in picks:
             n = reqs[i][3]
             hs = []
@@ -582,21 +613,41 @@ def run_serving(args):
             d = tv_distance(hs[0], hs[1])
             tvs.append({"request": i, "samples": n, "fp32_vs_fp64": d, "fp64_noise_floor": floor,
                         "ratio": d / floor if floor > 0 else None})
+    return {"value": binned / span, "unit": "samples/s", "span_s": span,
+            "iterated_per_s": iters / span, "offered_samples_per_s": offered,
+            "requests": len(reqs), "completed": len(results), "rate_per_s": rate,
+            "duration_s": duration, "seed": 23, "settle": 20, "traj_len": 4096,
+            "max_active": max_active,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                           "p99": float(np.percentile(lat, 99)),
+                           "p50_with_read": float(np.percentile(lat_read, 50)),
+                           "p99_with_read": float(np.percentile(lat_read, 99)),
+                           "by_kind_p50": {k: float(np.percentile(v, 50)) for k, v in kinds.items()},
+                           "by_kind_p99": {k: float(np.percentile(v, 99)) for k, v in kinds.items()}},
+            "wall_s": wall,
+            "tv": {"served_jobs": tvs,
+                   "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
+            "statuses": sorted({r[6] for r in results}), "errors": errors[:5],
+            "server_load": load, "clocks": clocks}
+
+
+def run_serving(args):
+    """Poisson request stream through the serving loop (ffr_server_*)."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    rec = serving_record(ffr, dev, args.rate, args.duration, args.warmup, args.max_active,
+                         with_tv=not args.no_tv)
     _line(args, f"Poisson serving stream, {args.rate:g} req/s for {args.duration:g} s "
-          "(80% 2-D, 15% 3-D, 5% continuations)", binned / span, span * 1e3, "f32",
-          {"requests": len(reqs), "completed": len(results), "rate_per_s": args.rate,
-           "duration_s": args.duration, "seed": 23, "settle": 20, "traj_len": 4096,
-           "max_active": args.max_active, "flush": "n/a (a stream of distinct buffers)"},
-          latency_ms={"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                      "p50_with_read": float(np.percentile(lat_read, 50)),
-                      "p99_with_read": float(np.percentile(lat_read, 99)),
-                      "by_kind_p50": {k: float(np.percentile(v, 50)) for k, v in kinds.items()},
-                      "by_kind_p99": {k: float(np.percentile(v, 99)) for k, v in kinds.items()}},
-          offered_samples_per_s=offered, iterated_per_s=iters / span, wall_s=wall,
-          tv={"served_jobs": tvs,
-              "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
-          statuses=sorted({r[6] for r in results}), errors=errors[:5],
-          server_load=load, clocks=clocks)
+          "(80% 2-D, 15% 3-D, 5% continuations)", rec["value"], rec["span_s"] * 1e3, "f32",
+          {k: rec[k] for k in ("requests", "completed", "rate_per_s", "duration_s", "seed",
+                               "settle", "traj_len", "max_active")}
+          | {"flush": "n/a (a stream of distinct buffers)"},
+          latency_ms=rec["latency_ms"], offered_samples_per_s=rec["offered_samples_per_s"],
+          iterated_per_s=rec["iterated_per_s"], wall_s=rec["wall_s"], tv=rec["tv"],
+          statuses=rec["statuses"], errors=rec["errors"], server_load=rec["server_load"],
+          clocks=rec["clocks"])
 
 
 def main():
@@ -617,6 +668,11 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--max-active", type=int, default=256)
+    ap.add_argument("--no-sub", action="store_true",
+                    help="default workload only: skip the batch and serving sub-records")
+    ap.add_argument("--serving-seconds", type=float, default=10.0,
+                    help="default workload: arrival window of the over-capacity stream "
+                         "(the sustainable one runs 1.5x as long)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted", "hot"],
                     help="render kernel (auto: the library's autotuner decides)")
     args = ap.parse_args()
@@ -719,15 +775,27 @@ def main():
         return
 
     peaks, peak_kind = measured_peaks()
-    per_launch_bytes = 8.0 * binned / launches
+    # per launch of the render kernel: one 4-byte atomic add per binned
+    # sample (8 B of read-modify-write), over the launch's average event time
+    per_launch_ops = binned / launches
     avg_s = kern_ms / launches * 1e-3
-    achieved = per_launch_bytes / avg_s / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                "traffic": profile_traffic(),
-                "peak_source": peak_kind,
-                "kernel": f"render kernel ({kernel_used}), FP32"}
+    achieved_hbm = 8.0 * per_launch_ops / avg_s / 1e9
     atom = ffr.measure_atomic_rate(1920 * 1080, 1 << 31, device=local)
+    traffic = profile_traffic()
+    # the primary bound: the 8.3 MB buffer is L2-resident, so binning is
+    # capped by the rate of L2 atomics, measured in this run
+    roofline = {"bound": "l2_atomic", "achieved": per_launch_ops / avg_s / 1e9,
+                "peak": atom / 1e9, "unit": "G atomic adds/s",
+                "frac": per_launch_ops / avg_s / atom,
+                "traffic": traffic, "traffic_unit": "DRAM bytes per launch (ncu)",
+                "peak_source": "measured in this run: u32 atomic adds at uniformly random "
+                               "cells of a 1920x1080 buffer (ffr_measure_atomic_rate)",
+                "kernel": f"render kernel ({kernel_used}), FP32"}
+    roofline_hbm = {"bound": "hbm", "achieved": achieved_hbm, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved_hbm / peaks["hbm_gbs"],
+                    "traffic": traffic, "peak_source": peak_kind,
+                    "what": "8 B per binned sample against the HBM copy bandwidth (of "
+                            f"{peak_kind}); secondary: every atomic resolves in L2"}
     l2 = {"peak_ops_per_s": atom, "achieved_ops_per_s": binned / (kern_ms * 1e-3),
           "frac": binned / (kern_ms * 1e-3) / atom,
           "what": "u32 atomic adds at uniformly random cells of a 1920x1080 buffer"}
@@ -758,7 +826,29 @@ def main():
         threads = os.cpu_count() or 1
         rate, irate, n, dt = cpu_port_rate(flame, settle, args.cpu_seconds, threads)
         cpu = {"value": rate, "unit": "samples/s", "cores": threads, "kind": "port",
-               "sample": f"{n} samples of the workload (FP64, settle 20), {dt:.1f} s"}
+               "sample": f"{n} samples of the workload (FP64, settle 20), {dt:.1f} s",
+               "port_vs_reference": PORT_VS_REFERENCE}
+
+    # the batched and serving paths (the 256-flame batch; the Poisson stream
+    # over capacity, then at 0.7x the capacity it measured), single GPU only
+    batch = serving = None
+    if ws == 1 and not args.no_sub:
+        batch = batch256_record(ffr, local, steps=2, warmup=1, with_tv=not args.no_tv)
+        over = serving_record(ffr, local, 200.0, args.serving_seconds, 1, args.max_active,
+                              with_tv=False)
+        per_req = over["offered_samples_per_s"] / over["rate_per_s"]
+        capacity = over["iterated_per_s"] / per_req
+        rate = round(0.7 * capacity, 1)
+        steady = serving_record(ffr, local, rate, args.serving_seconds * 1.5, 1,
+                                args.max_active, with_tv=not args.no_tv)
+        serving = {
+            "sustainable": dict(steady, what=f"0.7 x the measured capacity "
+                                f"({capacity:.1f} req/s = {over['iterated_per_s']:.3g} "
+                                f"samples/s / {per_req:.3g} samples per request)"),
+            "over_capacity": dict(over, what="200 req/s: offered samples/s above capacity, "
+                                  "so latency measures queue growth, not service time"),
+            "capacity_req_per_s": capacity,
+        }
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws,
@@ -776,6 +866,7 @@ def main():
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps},
         "gpu_launches": launches,
         "roofline": roofline,
+        "roofline_hbm": roofline_hbm,
         "l2_atomic": l2,
         "fp64": fp64,
         "tv": tv,
@@ -783,7 +874,13 @@ def main():
         "clocks": clocks,
         "iterated_per_s": iters / (kern_ms * 1e-3),
         "wall_s": wall_all,
+        "batch256": batch,
+        "serving": serving,
     }
+    if serving:
+        line["latency_ms"] = {"p50": serving["sustainable"]["latency_ms"]["p50"],
+                              "p99": serving["sustainable"]["latency_ms"]["p99"],
+                              "rate_per_s": serving["sustainable"]["rate_per_s"]}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -38,11 +38,13 @@ struct Prog
     const VarT<R>* var;
     const R* color;
     uint32_t present;       // ProgHeader::tier_a_present
+    uint32_t merged;        // ProgHeader::merged
 
     __device__ __forceinline__ void bind(const unsigned char* base)
     {
         h = reinterpret_cast<const ProgHeader<R>*>(base);
         present = h->tier_a_present;
+        merged = h->merged;
         thresh = reinterpret_cast<const uint64_t*>(base + h->off_thresh);
         xf = reinterpret_cast<const XformT<R>*>(base + h->off_xf);
         var = reinterpret_cast<const VarT<R>*>(base + h->off_var);
@@ -106,7 +108,15 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     for (int i = 0; i < D; ++i)
         v[i] = R(0);
     const int vb = x.var_begin, ve = x.var_begin + x.var_count;
-    if (pg.present == kTaLinear)
+    // FP32 programs in the merged form: each type once, weighted (falls
+    // through to the per-slot loop for points too large for it)
+    const bool merged = sizeof(R) == sizeof(float) && pg.merged
+        && merged_variations<D>(reinterpret_cast<const float*>(x.coef),
+                                reinterpret_cast<const float*>(t),
+                                reinterpret_cast<float*>(v), rng, pg.present);
+    if (merged)
+        ;
+    else if (pg.present == kTaLinear)
     {
         // every variation of the flame is linear (IFS fractals): v = sum of
         // w_j * t in the reference's accumulation order, no dispatch
@@ -186,10 +196,11 @@ __device__ __forceinline__ int pick_xform(const Prog<R>& pg, int nxf, Rng& rng)
 template <int D, typename R>
 __device__ __forceinline__ bool bad_point(const R* p)
 {
+    // |x| > threshold or NaN (utils/flame.hpp:26-29), as one unordered test
     bool b = false;
 #pragma unroll
     for (int i = 0; i < D; ++i)
-        b |= (RealTraits<R>::fabs_(p[i]) > RealTraits<R>::bad) || (p[i] != p[i]);
+        b |= !(RealTraits<R>::fabs_(p[i]) <= RealTraits<R>::bad);
     return b;
 }
 
@@ -494,8 +505,18 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
 #pragma unroll
                 for (int i = 0; i < D; ++i)
                 {
-                    ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
-                    ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
+                    if (sizeof(R) == sizeof(float))
+                    {
+                        // one min/max instruction each: the running extreme is
+                        // never NaN, and a NaN p keeps it, as the compare does
+                        ext_lo[i] = fminf(p[i], ext_lo[i]);
+                        ext_hi[i] = fmaxf(p[i], ext_hi[i]);
+                    }
+                    else
+                    {
+                        ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
+                        ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
+                    }
                 }
                 // bounds: inclusive [lo, hi]; NaN is out (documented deviation)
                 bool inb = true;

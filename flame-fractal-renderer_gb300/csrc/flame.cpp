@@ -385,6 +385,25 @@ std::vector<uint8_t> build_program(const HostFlame& f)
                 present |= bit;
             }
     h.tier_a_present = present;
+    // the FP32 merged form: every type once per application, weighted by
+    // the xform's summed weight of that type.  Sums of equal terms are the
+    // same map (V(t) does not depend on the instance), except julia, whose
+    // random word differs per instance.
+    h.merged = 0;
+    if (sizeof(R) == sizeof(float) && !(present & (1u << 7))
+            && (f.dims == 2 || !(present & 0x78u)))
+    {
+        bool ok = true;
+        for (const HostXform* x : all)
+            if (x)
+            {
+                int jul = 0;
+                for (const auto& v : x->vars)
+                    jul += v.type == V_JULIA;
+                ok = ok && jul <= 1;
+            }
+        h.merged = ok ? 1 : 0;
+    }
     for (int i = 0; i < f.dims; ++i)
     {
         h.size[i] = f.size[i];
@@ -417,6 +436,16 @@ std::vector<uint8_t> build_program(const HostFlame& f)
         if (!x)
             continue;
         pack_xform<R>(*x, f.dims, xp[k], vb);
+        if (h.merged)
+            for (const auto& v : x->vars)
+            {
+                for (int t = 0; t < 7; ++t)
+                    if (v.type == kTierA[t])
+                        xp[k].coef[t] = (R)((double)xp[k].coef[t] + v.weight);
+                // julia draws its word whatever its weight
+                if (v.type == V_JULIA)
+                    xp[k].coef[7] = R(1);
+            }
         for (const auto& v : x->vars)
         {
             VarT<R>& d = vp[vb++];

@@ -48,6 +48,12 @@ struct alignas(16) XformT
     uint8_t has_post;
     uint8_t has_color;
     uint8_t rng_words;      // RNG words one application draws (fixed per xform)
+    // merged form (ProgHeader::merged): the summed weight of each benchmark
+    // variation type in this xform, in the order linear, sinusoidal,
+    // spherical, swirl, horseshoe, polar, julia (0 where the xform lacks
+    // the type), then 1 if the xform has julia (which draws a word even at
+    // weight 0), else 0
+    R coef[8];
 };
 
 template <typename R>
@@ -83,6 +89,13 @@ struct alignas(16) ProgHeader
     // application (lanes of a warp then consume their ISAAC blocks out of
     // phase and the render kernels keep a carry area for refill ahead)
     uint32_t draws_vary;
+    // 1 when the FP32 kernels evaluate each variation type once per xform
+    // application and weight it by XformT::coef (variations.cuh,
+    // merged_variations): FP32 programs whose variations are all benchmark
+    // types, with 2-D types only in 2-D flames and julia at most once per
+    // xform.  FP64 programs keep the reference's per-variation order.
+    uint32_t merged;
+    uint32_t pad_;
     uint64_t size[kMaxDims];
     uint64_t mult_i[kMaxDims];
     uint64_t cells;

@@ -361,6 +361,92 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
     }
 }
 
+// The merged form of an FP32 xform application (ProgHeader::merged):
+// v = sum over the flame's types T of coef[T] * V_T(t), each type evaluated
+// once whatever the number of variation slots, instead of one evaluation
+// (of every type present, then a select) per slot.  The types' formulas are
+// those of variation_tier_a; only the order of the weighted sum differs
+// from the reference's slot order, which FP32 rounding already departs
+// from.  A type the xform lacks has coef 0 and contributes 0 * V_T(t) = 0
+// because every V_T is finite while sum t_i^2 < 1e36; beyond that (and for
+// NaN) the function returns false and the caller evaluates the slots one by
+// one, so an infinite or NaN point propagates exactly as per-slot
+// evaluation propagates it.  Julia draws its word only in lanes whose xform
+// has julia (coef[7], even at weight 0), at the same point of the sequence
+// as the per-slot loop (the xform's only drawing variation, so its place
+// among the slots does not matter).
+template <int D, typename Rng>
+__device__ __forceinline__ bool merged_variations(const float* coef, const float* t, float* v,
+                                                  Rng& rng, uint32_t present)
+{
+    using T = RealTraits<float>;
+    const float4 c0 = *reinterpret_cast<const float4*>(coef);
+    const float4 c1 = *reinterpret_cast<const float4*>(coef + 4);
+    const float q = nsq<D>(t);
+    if (!(q < 1e36f))
+        return false;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        v[i] = 0.0f;
+    if (present & kTaLinear)                                     /* linear 169-177 */
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] = c0.x * t[i];
+    if (present & kTaSinusoidal)                                 /* sinusoidal 183-191 */
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] = fmaf(c0.y, T::sin_(t[i]), v[i]);
+    if (present & kTaSpherical)                                  /* spherical 197-208 */
+    {
+        const float k = c0.z * T::recip_(q + T::eps);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] = fmaf(k, t[i], v[i]);
+    }
+    if (D == 2 && (present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+    {
+        const float x = t[0], y = t[D - 1];
+        float rt = 0.0f, ang = 0.0f;
+        if (present & (kTaHorseshoe | kTaPolar | kTaJulia))
+            rt = T::sqrt_(q);
+        if (present & (kTaPolar | kTaJulia))
+            ang = T::atan2_(y, x);
+        float X = v[0], Y = v[D - 1];
+        if (present & kTaSwirl)                                  /* swirl 509-522 */
+        {
+            float s, c;
+            T::sincos_(q, &s, &c);
+            X = fmaf(c0.w, x * s - y * c, X);
+            Y = fmaf(c0.w, x * c + y * s, Y);
+        }
+        if (present & kTaHorseshoe)                              /* horseshoe 527-540 */
+        {
+            const float k = c1.x * T::recip_(rt + T::eps);
+            X = fmaf(k, (x - y) * (x + y), X);
+            Y = fmaf(k, 2.0f * x * y, Y);
+        }
+        if (present & kTaPolar)                                  /* polar 545-555 */
+        {
+            X = fmaf(c1.y, ang * T::inv_pi, X);
+            Y = fmaf(c1.y, rt - 1.0f, Y);
+        }
+        if (present & kTaJulia)                                  /* julia 807-819 */
+        {
+            float bit = 0.0f;
+            if (c1.w != 0.0f)
+                bit = (rng.next() & 1u) ? 1.0f : 0.0f;
+            float s, c;
+            T::sincos_(0.5f * ang + bit * T::pi, &s, &c);
+            const float k = c1.z * rt;
+            X = fmaf(k, c, X);
+            Y = fmaf(k, s, Y);
+        }
+        v[0] = X;
+        v[D - 1] = Y;
+    }
+    return true;
+}
+
 // one variation: o = V(t).  Restates each class of
 // src/variations/variations.hpp (line numbers in the case comments) in the
 // reference's operation order; Point / k is multiplication by (1/k), as

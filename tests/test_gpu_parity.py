@@ -40,6 +40,15 @@ def tv(a, b):
     return 0.5 * np.abs(a / a.sum() - b / b.sum()).sum()
 
 
+def oracle_floor_pair(case):
+    """Two oracle renders of a golden render case with seeds other than the
+    case's: their TV distance is the case's noise floor."""
+    import flame_oracle as fo
+    of = fo.OracleFlame(fo.load_flame(golden_flame_text(case["flame"])))
+    return [fo.render(of, case["seed"] + k, case["streams"], case["samples"], case["traj_len"],
+                      case["settle"], case["bad_limit"], threads=8) for k in (1000, 2000)]
+
+
 @pytest.mark.parametrize("key", MAN["kat"]["keys"])
 def test_isaac_words_match_reference(ffr, key):
     want = npz("kat")[f"k{key}"]
@@ -143,8 +152,14 @@ def test_render_fp64_matches_reference(ffr, case, kernel):
             col = buf[:, 1:].copy().view(np.float64)
             np.testing.assert_allclose(col, d["colors"], rtol=1e-12, atol=1e-9)
     else:
-        assert abs(int(counts.sum()) - int(d["counts"].sum())) <= 0.02 * d["counts"].sum() + 50
-        assert tv(counts, d["counts"]) < 0.2
+        # chaotic through libm: the reference's run (the golden, this seed)
+        # against ours by TV, within 3x the TV between two oracle runs of
+        # the same case with other seeds
+        a, b = oracle_floor_pair(case)
+        floor = tv(a.counts, b.counts)
+        assert tv(counts, d["counts"]) <= 3.0 * floor, (tv(counts, d["counts"]), floor)
+        spread = abs(int(a.counts.sum()) - int(b.counts.sum()))
+        assert abs(int(counts.sum()) - int(d["counts"].sum())) <= 3 * spread + 50
 
 
 @pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)

@@ -1,6 +1,9 @@
 """ffr-img side: the device pixel mapping (ffr_render_image), the host PNG
 writer (ffr_encode_png) and the ffr-img command line, checked against the
-CPU restatement of the reference's render_image (oracle/image_oracle.py).
+reference's own ffr-img pixels (tests/golden/data/images.npz, made by
+tests/golden/make_golden_images.py from src/ffr_img.cpp compiled into the
+oracle) and against the CPU restatement of its render_image
+(oracle/image_oracle.py), which is itself checked against those pixels.
 
 The pixel mapping runs log and pow in double on the GPU; the oracle uses
 numpy's.  They can differ by an ulp, which moves a pixel by one level only
@@ -60,6 +63,38 @@ def test_cli_argument_errors(ffr, tmp_path, args, msg):
     assert r.returncode == 1 and msg in r.stderr
 
 
+GOLDEN_IMAGES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+with open(os.path.join(GOLDEN_IMAGES, "images.json")) as _f:
+    IMAGES = json.load(_f)
+
+
+def golden_image_case(name):
+    """(flame text, buffer as u64 [cells, 1 + colour dims], mode, gamma,
+    bits, reference pixels) of one golden image case."""
+    d = np.load(os.path.join(GOLDEN_IMAGES, "data", "images.npz"))
+    m = IMAGES["images"][name]
+    flame = IMAGES["buffers"][m["buffer"]]["flame"]
+    text = golden_flame_text(flame)
+    r = json.loads(text).get("color_dimensions", 0)
+    buf = d["buf_" + m["buffer"]].reshape(-1, 1 + r)
+    opts = m["options"]
+    mode = io.RGB if "-c" in opts else (io.MONO if "-m" in opts else io.GRAY)
+    gamma = float(opts[opts.index("-y") + 1]) if "-y" in opts else 1.0
+    bits = int(opts[opts.index("-b") + 1]) if "-b" in opts else 8
+    return text, buf, mode, gamma, bits, d["img_" + name]
+
+
+@pytest.mark.parametrize("name", sorted(IMAGES["images"]))
+def test_image_oracle_matches_reference_pixels(name):
+    """The numpy restatement against the reference's own ffr-img output."""
+    text, buf, mode, gamma, bits, want = golden_image_case(name)
+    w, h = json.loads(text)["size"]
+    colors = buf[:, 1:].copy().view(np.float64) if buf.shape[1] > 1 else None
+    got, _ = io.image(buf[:, 0], colors, w, h, mode, gamma, bits)
+    assert got.shape == want.shape and got.dtype == want.dtype
+    _close(got, want)
+
+
 def _close(got, want):
     d = np.abs(got.astype(np.int64) - want.astype(np.int64))
     assert d.max() <= 1, d.max()
@@ -83,6 +118,40 @@ def test_render_image_matches_oracle(ffr, flames, mode, bits, gamma):
     assert info.scale_max == pytest.approx(b["scale_max"], rel=1e-15)
     assert px.shape == want.shape and px.dtype == want.dtype
     _close(px, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(IMAGES["images"]))
+def test_render_image_matches_reference_pixels(ffr, name):
+    """The device pixel mapping of a buffer the reference rendered, against
+    the pixels the reference's own ffr-img made of it."""
+    text, buf, mode, gamma, bits, want = golden_image_case(name)
+    with ffr.BufferRenderer(text, precision=0, settle=20) as r:
+        r.load_buffer(buf)
+        px, info = r.render_image(mode, gamma, bits)
+    assert (info.hist_min, info.hist_max) == (int(buf[:, 0].min()), int(buf[:, 0].max()))
+    assert px.shape == want.shape and px.dtype == want.dtype
+    _close(px, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c2small_gray16_g045", "color_rgb8", "c2small_mono"])
+def test_ffr_img_cli_matches_reference_pixels(ffr, tmp_path, name):
+    """ffr-img on the same buffer file: the PNG decodes to the reference's
+    pixels, and the bounds lines match the reference's stderr."""
+    text, buf, mode, gamma, bits, want = golden_image_case(name)
+    m = IMAGES["images"][name]
+    f = tmp_path / "flame.json"
+    f.write_text(text)
+    b = tmp_path / "in.buf"
+    buf.tofile(b)
+    png = tmp_path / "out.png"
+    r = subprocess.run([ffr.IMG_CLI_PATH, "-f", str(f), "-i", str(b), "-o", str(png),
+                        *m["options"]], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for line in m["stderr_bounds"]:
+        assert line in r.stderr
+    _close(io.decode_png(png.read_bytes()), want)
 
 
 @pytest.mark.gpu
