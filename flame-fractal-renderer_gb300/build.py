@@ -72,7 +72,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs = []   # (target, deps, cmd)
     for p in (0, 1):
         for d in (1, 2, 3):
-            for kind in range(6):
+            for kind in range(8 if p == 1 else 6):
                 obj = os.path.join(OUT, f"chaos_p{p}_d{d}_k{kind}.o")
                 src = os.path.join(CSRC, "chaos_inst.cu")
                 extra = ["--fmad=false"] if p == 0 else []

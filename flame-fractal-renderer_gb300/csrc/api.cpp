@@ -346,7 +346,8 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     }
     const bool use_hot = want_hot && k == FFR_KERNEL_PLAIN;
     if (k == FFR_KERNEL_PLAIN)
-        CU(c, c->L().occ(color, rsl_words_for(c->prog_host.data()), use_hot ? 1 : 0, &bps,
+        CU(c, c->L().occ(color, merged_for(c->prog_host.data()),
+                         rsl_words_for(c->prog_host.data()), use_hot ? 1 : 0, &bps,
                          &block, pb, nxf, &smem));
     *kernel = k;
     if (bps < 1)
@@ -429,6 +430,7 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
     a.rng_words = program_words(c);
     a.agg = agg;
     a.rsl_words = rsl_words_for(c->prog_host.data());
+    a.merged = merged_for(c->prog_host.data());
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
     set_geometry(a, c->prog_host.data(), c->opts.precision);
 }
@@ -1369,7 +1371,7 @@ struct ffr_batch
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     struct Group
     {
-        int dims = 0, color = 0;
+        int dims = 0, color = 0, merged = 0;
         std::vector<int> members;
         JobDesc* d_jobs = nullptr;          // njobs JobDesc + BatchHead
         BatchHead* d_head = nullptr;
@@ -1453,7 +1455,7 @@ cudaError_t batch_capture(ffr_batch* b, ffr_batch::Group& g)
     if (e != cudaSuccess)
         return e;
     cudaError_t e1 = launch_batch_reset(g.d_jobs, ba.njobs, g.d_head, b->stream);
-    cudaError_t e2 = L.batch(ba, g.color, g.grid, g.smem, b->stream);
+    cudaError_t e2 = L.batch(ba, g.color, g.merged, g.grid, g.smem, b->stream);
     e = cudaStreamEndCapture(b->stream, &graph);
     if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess)
     {
@@ -1522,13 +1524,15 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
         return cfail(e, "cudaStreamCreate");
     if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess)
         return cfail(e, "cudaEventCreate");
-    // group by (dims, colour): one persistent kernel instantiation each
+    // group by (dims, colour, merged form): one persistent kernel
+    // instantiation each
     for (size_t i = 0; i < n; ++i)
     {
         const int d = ctxs[i]->flame.dims, col = ctxs[i]->flame.color_dims > 0;
+        const int mg = merged_for(ctxs[i]->prog_host.data());
         ffr_batch::Group* g = nullptr;
         for (auto& x : b->groups)
-            if (x.dims == d && x.color == col)
+            if (x.dims == d && x.color == col && x.merged == mg)
                 g = &x;
         if (!g)
         {
@@ -1536,6 +1540,7 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
             g = &b->groups.back();
             g->dims = d;
             g->color = col;
+            g->merged = mg;
         }
         g->members.push_back((int)i);
     }
@@ -1563,13 +1568,14 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
             const int hot = c->hot_mult != 0;
             g.hot.push_back((char)hot);
             size_t sm = 0;
-            if ((e = L.occ(g.color, rsl_words_for(c->prog_host.data()), hot, &bps, &block,
+            if ((e = L.occ(g.color, g.merged, rsl_words_for(c->prog_host.data()), hot, &bps,
+                           &block,
                            (unsigned int)c->prog_host.size(),
                            (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
                 return cfail(e, "occupancy");
             g.smem = std::max(g.smem, sm);
         }
-        if ((e = L.occ_batch(g.color, &bps, &block, g.smem)) != cudaSuccess)
+        if ((e = L.occ_batch(g.color, g.merged, &bps, &block, g.smem)) != cudaSuccess)
             return cfail(e, "batch occupancy");
         if (bps < 1)
         {

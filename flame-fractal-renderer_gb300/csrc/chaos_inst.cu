@@ -1,21 +1,24 @@
 // Instantiates the chaos kernels for one (precision, dims) pair; compiled
 // once per pair and kind with -DFFR_P=<0|1> -DFFR_D=<1|2|3>
-// -DFFR_KIND=<0..5>, so the objects compile in parallel:
+// -DFFR_KIND=<0..7>, so the objects compile in parallel:
 //   0  plain render kernel without colour (and the colour dispatch)
 //   1  xform-sorted render kernel
 //   2  plain render kernel with colour
 //   3  persistent batch kernel without colour (and the colour dispatch)
 //   4  persistent batch kernel with colour
 //   5  single-step and trace kernels
-// Each render kernel inlines every variation, so one kernel per object keeps
-// the slowest object (FP64 without contraction) short.  The FP64 objects are
+//   6  FP32 only: plain render kernels for merged-form programs (both colour
+//      variants; ProgHeader::merged, only the seven benchmark variations)
+//   7  FP32 only: persistent batch kernels for merged-form programs
+// Each general render kernel inlines every variation, so one kernel per
+// object keeps the slowest object (FP64 without contraction) short.  The FP64 objects are
 // built with --fmad=false so no multiply-add is contracted: the reference
 // (and the oracle) round every product and sum separately.
 #include "chaos_kernel.cuh"
 #include "chaos_sorted.cuh"
 
 #if !defined(FFR_P) || !defined(FFR_D) || !defined(FFR_KIND)
-#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3> -DFFR_KIND=<0..5>"
+#error "compile with -DFFR_P=<0|1> -DFFR_D=<1|2|3> -DFFR_KIND=<0..7>"
 #endif
 
 #define FFR_CAT2(a, b, c, d) a##_p##b##_d##c##d
@@ -37,17 +40,24 @@ cudaError_t FFR_NAME(occupancy_color)(int rsl_words, int hot, int* blocks_per_sm
 cudaError_t FFR_NAME(launch_batch_color)(const BatchArgs& b, int grid, size_t smem,
                                          cudaStream_t st);
 cudaError_t FFR_NAME(occupancy_batch_color)(int* blocks_per_sm, size_t smem);
+// the merged-form instantiations (FP32, kinds 6 and 7)
+cudaError_t FFR_NAME(launch_render_merged)(const RenderArgs& a, int grid, cudaStream_t st);
+cudaError_t FFR_NAME(occupancy_merged)(int color, int rsl_words, int hot, int* blocks_per_sm,
+                                       unsigned int prog_bytes, int nxf, size_t* smem);
+cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int grid, size_t smem,
+                                          cudaStream_t st);
+cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int* blocks_per_sm, size_t smem);
 
 constexpr int kBlock = 128;
 
-#if FFR_KIND == 0 || FFR_KIND == 2
+#if FFR_KIND == 0 || FFR_KIND == 2 || FFR_KIND == 6
 
-template <bool C>
+template <bool C, bool M = false>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf, a.rsl_words,
                                                  a.hot_keys != nullptr);
-    auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock, M>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -56,12 +66,12 @@ static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <bool C>
+template <bool C, bool M = false>
 static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_words, int hot,
                            size_t* smem_out)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf, rsl_words, hot != 0);
-    auto k = chaos_kernel<FFR_D, Real, C, kBlock>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock, M>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -76,14 +86,26 @@ static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_w
 
 cudaError_t FFR_NAME(launch_render)(const RenderArgs& a, int grid, cudaStream_t st)
 {
+#if FFR_P == 1
+    if (a.merged)
+        return FFR_NAME(launch_render_merged)(a, grid, st);
+#endif
     return a.color_dims > 0 ? FFR_NAME(launch_render_color)(a, grid, st)
                             : launch_one<false>(a, grid, st);
 }
 
-cudaError_t FFR_NAME(occupancy)(int color, int rsl_words, int hot, int* blocks_per_sm,
-                                int* block, unsigned int prog_bytes, int nxf, size_t* smem)
+cudaError_t FFR_NAME(occupancy)(int color, int merged, int rsl_words, int hot,
+                                int* blocks_per_sm, int* block, unsigned int prog_bytes,
+                                int nxf, size_t* smem)
 {
     *block = kBlock;
+#if FFR_P == 1
+    if (merged)
+        return FFR_NAME(occupancy_merged)(color, rsl_words, hot, blocks_per_sm, prog_bytes, nxf,
+                                          smem);
+#else
+    (void)merged;
+#endif
     return color ? FFR_NAME(occupancy_color)(rsl_words, hot, blocks_per_sm, prog_bytes, nxf, smem)
                  : occ_one<false>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
 }
@@ -101,47 +123,94 @@ cudaError_t FFR_NAME(occupancy_color)(int rsl_words, int hot, int* blocks_per_sm
     return occ_one<true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
 }
 
-#elif FFR_KIND == 3 || FFR_KIND == 4
+#elif FFR_KIND == 6 && FFR_P == 1
 
-template <bool C>
+cudaError_t FFR_NAME(launch_render_merged)(const RenderArgs& a, int grid, cudaStream_t st)
+{
+    return a.color_dims > 0 ? launch_one<true, true>(a, grid, st)
+                            : launch_one<false, true>(a, grid, st);
+}
+
+cudaError_t FFR_NAME(occupancy_merged)(int color, int rsl_words, int hot, int* blocks_per_sm,
+                                       unsigned int prog_bytes, int nxf, size_t* smem)
+{
+    return color ? occ_one<true, true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
+                 : occ_one<false, true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
+}
+
+#endif
+
+#if FFR_KIND == 3 || FFR_KIND == 4 || FFR_KIND == 7
+
+template <bool C, bool M = false>
 static cudaError_t batch_attr(size_t smem)
 {
-    return cudaFuncSetAttribute(chaos_batch_kernel<FFR_D, Real, C, kBlock>,
+    return cudaFuncSetAttribute(chaos_batch_kernel<FFR_D, Real, C, kBlock, M>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <bool C>
+template <bool C, bool M = false>
 static cudaError_t batch_launch(const BatchArgs& b, int grid, size_t smem, cudaStream_t st)
 {
-    chaos_batch_kernel<FFR_D, Real, C, kBlock><<<grid, kBlock, smem, st>>>(b);
+    chaos_batch_kernel<FFR_D, Real, C, kBlock, M><<<grid, kBlock, smem, st>>>(b);
     return cudaGetLastError();
 }
 
-template <bool C>
+template <bool C, bool M = false>
 static cudaError_t batch_occ(int* blocks_per_sm, size_t smem)
 {
-    cudaError_t e = batch_attr<C>(smem);
+    cudaError_t e = batch_attr<C, M>(smem);
     if (e != cudaSuccess)
         return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        blocks_per_sm, chaos_batch_kernel<FFR_D, Real, C, kBlock>, kBlock, smem);
+        blocks_per_sm, chaos_batch_kernel<FFR_D, Real, C, kBlock, M>, kBlock, smem);
 }
 
 #if FFR_KIND == 3
 
-cudaError_t FFR_NAME(launch_batch)(const BatchArgs& b, int color, int grid, size_t smem,
-                                   cudaStream_t st)
+cudaError_t FFR_NAME(launch_batch)(const BatchArgs& b, int color, int merged, int grid,
+                                   size_t smem, cudaStream_t st)
 {
+#if FFR_P == 1
+    if (merged)
+        return FFR_NAME(launch_batch_merged)(b, color, grid, smem, st);
+#else
+    (void)merged;
+#endif
     return color ? FFR_NAME(launch_batch_color)(b, grid, smem, st)
                  : batch_launch<false>(b, grid, smem, st);
 }
 
-cudaError_t FFR_NAME(occupancy_batch)(int color, int* blocks_per_sm, int* block, size_t smem)
+cudaError_t FFR_NAME(occupancy_batch)(int color, int merged, int* blocks_per_sm, int* block,
+                                      size_t smem)
 {
     *block = kBlock;
+#if FFR_P == 1
+    if (merged)
+        return FFR_NAME(occupancy_batch_merged)(color, blocks_per_sm, smem);
+#else
+    (void)merged;
+#endif
     return color ? FFR_NAME(occupancy_batch_color)(blocks_per_sm, smem)
                  : batch_occ<false>(blocks_per_sm, smem);
 }
+
+#elif FFR_KIND == 7
+
+#if FFR_P == 1
+cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int grid, size_t smem,
+                                          cudaStream_t st)
+{
+    return color ? batch_launch<true, true>(b, grid, smem, st)
+                 : batch_launch<false, true>(b, grid, smem, st);
+}
+
+cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int* blocks_per_sm, size_t smem)
+{
+    return color ? batch_occ<true, true>(blocks_per_sm, smem)
+                 : batch_occ<false, true>(blocks_per_sm, smem);
+}
+#endif
 
 #else
 

@@ -91,7 +91,11 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
 
 // XForm::applyIteration (xform.hpp:211-227).  For dims < 3 both affines are
 // always applied (identity when absent), for dims >= 3 only when present.
-template <int D, typename R, typename Rng>
+// MERGED: the instantiation for FP32 programs in the merged form
+// (ProgHeader::merged), which contain only the seven benchmark types; it
+// carries no code for the other 91 (smaller kernels, no stack frame) and
+// computes exactly what the general instantiation computes for them.
+template <int D, typename R, bool MERGED = false, typename Rng>
 __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& x,
                                             const R* p, R* out, Rng& rng)
 {
@@ -110,7 +114,7 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     const int vb = x.var_begin, ve = x.var_begin + x.var_count;
     // FP32 programs in the merged form: each type once, weighted (falls
     // through to the per-slot loop for points too large for it)
-    const bool merged = sizeof(R) == sizeof(float) && pg.merged
+    const bool merged = sizeof(R) == sizeof(float) && (MERGED || pg.merged)
         && merged_variations<D>(reinterpret_cast<const float*>(x.coef),
                                 reinterpret_cast<const float*>(t),
                                 reinterpret_cast<float*>(v), rng, pg.present);
@@ -150,7 +154,10 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
         {
             const VarT<R>& var = pg.var[k];
             R o[D];
-            variation<D, R>(var, t, o, rng, pg.present, pp);
+            if (MERGED)
+                variation_tier_a<D, R>(var, t, o, rng, pg.present, pp);
+            else
+                variation<D, R>(var, t, o, rng, pg.present, pp);
             const R w = var.weight;
 #pragma unroll
             for (int i = 0; i < D; ++i)
@@ -292,7 +299,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi, unsi
 
 // Runs streams s_first, s_first + s_stride, ... (below the job's active
 // stream count), then merges this CTA's statistics into a.stats.
-template <int D, typename R, bool COLOR, int BLOCK>
+template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
 __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem,
                                            unsigned long long s_first,
                                            unsigned long long s_stride)
@@ -413,7 +420,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     refill_ahead();
                     const int xi = pick_xform<R>(pg, nxf, rng);
                     R q[D];
-                    apply_xform<D, R>(pg, pg.xf[xi], p, q, rng);
+                    apply_xform<D, R, MERGED>(pg, pg.xf[xi], p, q, rng);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -431,7 +438,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
-                    apply_xform<D, R>(pg, xf, p, q, rng);
+                    apply_xform<D, R, MERGED>(pg, xf, p, q, rng);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -446,7 +453,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 if (h.has_final)
                 {
                     const XformT<R>& ff = pg.xf[nxf];
-                    apply_xform<D, R>(pg, ff, p, pf, rng);
+                    apply_xform<D, R, MERGED>(pg, ff, p, pf, rng);
                     if (COLOR)
                     {
                         if (ff.has_color)
@@ -665,14 +672,15 @@ __host__ __device__ constexpr int render_min_blocks()
     return sizeof(R) == 4 ? 6 : 4;
 }
 
-template <int D, typename R, bool COLOR, int BLOCK>
+template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
 __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
     __syncthreads();
-    chaos_body<D, R, COLOR, BLOCK>(a, smem, (unsigned long long)blockIdx.x * BLOCK + threadIdx.x,
-                                   (unsigned long long)gridDim.x * BLOCK);
+    chaos_body<D, R, COLOR, BLOCK, MERGED>(a, smem,
+                                           (unsigned long long)blockIdx.x * BLOCK + threadIdx.x,
+                                           (unsigned long long)gridDim.x * BLOCK);
 }
 
 // Persistent multi-flame render: each CTA claims (job, chunk of BLOCK
@@ -682,7 +690,7 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(co
 // so every job's buffer is the same alone and in the batch.  The claimed
 // job's arguments are copied to shared memory and its program is reloaded
 // only when the CTA moves to another job.
-template <int D, typename R, bool COLOR, int BLOCK>
+template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
 __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_kernel(const BatchArgs b)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -720,8 +728,8 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_ker
             __syncthreads();
             cur = j;
         }
-        chaos_body<D, R, COLOR, BLOCK>(s_args, smem, s_chunk * BLOCK + threadIdx.x,
-                                       ~0ull >> 1);
+        chaos_body<D, R, COLOR, BLOCK, MERGED>(s_args, smem, s_chunk * BLOCK + threadIdx.x,
+                                               ~0ull >> 1);
         __syncthreads();
     }
 }

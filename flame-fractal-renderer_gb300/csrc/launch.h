@@ -55,6 +55,9 @@ struct RenderArgs
     int rng_words;                  // largest RNG draw of one xform (sorted kernel)
     int agg;                        // warp-aggregate increments of equal cells
     int rsl_words;                  // ISAAC result array words (16 or kIsaacRslMax)
+    // the program is in the FP32 merged form (ProgHeader::merged): the
+    // launch runs the instantiation without the other 91 variations
+    int merged;
     // hot-cell table of the plain kernel (kHotSlots keys), or null; needs
     // fewer than 2^30 cells and fewer than 2^32 samples per CTA
     const unsigned int* hot_keys;
@@ -127,6 +130,17 @@ inline int rsl_words_for(const void* prog)
 }
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
+
+// ProgHeader::merged of a program blob (0 for FP64 programs)
+inline int merged_for(const void* prog)
+{
+    static_assert(offsetof(ProgHeader<double>, merged) == offsetof(ProgHeader<float>, merged),
+                  "program header layout");
+    uint32_t v = 0;
+    memcpy(&v, static_cast<const unsigned char*>(prog) + offsetof(ProgHeader<double>, merged),
+           sizeof v);
+    return v ? 1 : 0;
+}
 
 // Hot cells: a flame's density can sit largely in a few cells (fixed
 // points, attractor cores; the 1920x1080 benchmark flame puts 18% of its
@@ -295,8 +309,8 @@ inline int agg_after_search(bool searched) { return searched ? 0 : kDefaultAgg; 
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \
     cudaError_t launch_render_p##P##_d##D(const RenderArgs&, int grid,          \
                                           cudaStream_t);                        \
-    cudaError_t occupancy_p##P##_d##D(int color, int rsl_words, int hot,        \
-                                      int* blocks_per_sm, int* block,           \
+    cudaError_t occupancy_p##P##_d##D(int color, int merged, int rsl_words,     \
+                                      int hot, int* blocks_per_sm, int* block,  \
                                       unsigned int prog_bytes, int nxf,         \
                                       size_t* smem);                            \
     cudaError_t launch_sorted_p##P##_d##D(const RenderArgs&, int grid,          \
@@ -305,10 +319,12 @@ inline int agg_after_search(bool searched) { return searched ? 0 : kDefaultAgg; 
                                              int* blocks_per_sm, int* block,    \
                                              unsigned int prog_bytes, int nxf,  \
                                              int words, size_t* smem);          \
-    cudaError_t launch_batch_p##P##_d##D(const BatchArgs&, int color, int grid, \
-                                         size_t smem, cudaStream_t);            \
-    cudaError_t occupancy_batch_p##P##_d##D(int color, int* blocks_per_sm,      \
-                                            int* block, size_t smem);           \
+    cudaError_t launch_batch_p##P##_d##D(const BatchArgs&, int color,           \
+                                         int merged, int grid, size_t smem,     \
+                                         cudaStream_t);                         \
+    cudaError_t occupancy_batch_p##P##_d##D(int color, int merged,              \
+                                            int* blocks_per_sm, int* block,     \
+                                            size_t smem);                       \
     cudaError_t launch_step_p##P##_d##D(const StepArgs&, cudaStream_t);         \
     cudaError_t launch_trace_p##P##_d##D(const TraceArgs&, cudaStream_t);
 
@@ -320,12 +336,12 @@ FFR_DECLARE_LAUNCHERS(1, 2)
 FFR_DECLARE_LAUNCHERS(1, 3)
 
 typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
-typedef cudaError_t (*OccFn)(int, int, int, int*, int*, unsigned int, int, size_t*);
+typedef cudaError_t (*OccFn)(int, int, int, int, int*, int*, unsigned int, int, size_t*);
 typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
 typedef cudaError_t (*TraceFn)(const TraceArgs&, cudaStream_t);
 typedef cudaError_t (*OccSortedFn)(int, int, int*, int*, unsigned int, int, int, size_t*);
-typedef cudaError_t (*BatchFn)(const BatchArgs&, int, int, size_t, cudaStream_t);
-typedef cudaError_t (*OccBatchFn)(int, int*, int*, size_t);
+typedef cudaError_t (*BatchFn)(const BatchArgs&, int, int, int, size_t, cudaStream_t);
+typedef cudaError_t (*OccBatchFn)(int, int, int*, int*, size_t);
 
 // the launch functions of one (precision, dims) kernel instantiation
 struct Launchers

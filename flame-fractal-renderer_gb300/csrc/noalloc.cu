@@ -207,7 +207,8 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     const int nxf = (int)f.xforms.size();
     int bps = 0, block = 0, sms = 1;
     size_t smem = 0;
-    if ((e = occ(f.color_dims > 0, rsl_words_for(prog.data()), 0, &bps, &block,
+    if ((e = occ(f.color_dims > 0, merged_for(prog.data()), rsl_words_for(prog.data()), 0,
+                 &bps, &block,
                  (unsigned int)prog.size(), nxf, &smem))
             != cudaSuccess)
         return nocuda(e, "occupancy");
@@ -264,6 +265,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     a.stats = dstats;
     a.cancel = nullptr;
     a.rsl_words = rsl_words_for(prog.data());
+    a.merged = merged_for(prog.data());
     isaac_init_table(a.isaac_init);
     set_geometry(a, prog.data(), o.precision);
     const auto t0 = std::chrono::steady_clock::now();

@@ -46,7 +46,9 @@ namespace {
 
 constexpr int kChunkStreams = 128;          // BLOCK of the batch kernel
 constexpr int kRoundSlots = 2;
-constexpr int kGroups = 6;                  // dims 1..3 x colour off/on
+// dims 1..3 x merged form (FP32 programs of the seven benchmark variations)
+// off/on x colour off/on: group g = ((dims - 1) * 2 + merged) * 2 + colour
+constexpr int kGroups = 12;
 constexpr size_t kStagingBytes = 16u << 20; // device staging of one read slot
 constexpr int kReadSlots = 4;               // concurrent buffer reads
 
@@ -394,8 +396,9 @@ bool Server::launch_round_locked()
     {
         int bps = 0, block = 0;
         const SrvBuffer& b0 = *cand.front()->buf;
-        launchers(o.precision, b0.flame.dims).occ_batch(b0.flame.color_dims > 0, &bps, &block,
-                                                        b0.smem);
+        launchers(o.precision, b0.flame.dims).occ_batch(b0.flame.color_dims > 0,
+                                                        merged_for(b0.prog.data()), &bps,
+                                                        &block, b0.smem);
         budget_chunks = 2ull * (uint64_t)sms * (uint64_t)std::max(1, bps);
     }
     budget_chunks = std::min<uint64_t>(budget_chunks, r->order_cap);
@@ -430,7 +433,8 @@ bool Server::launch_round_locked()
                 continue;
             SrvJob* j = cand[i];
             const SrvBuffer& b = *j->buf;
-            const int gi = (b.flame.dims - 1) * 2 + (b.flame.color_dims > 0);
+            const int gi = ((b.flame.dims - 1) * 2 + merged_for(b.prog.data())) * 2
+                + (b.flame.color_dims > 0);
             if (gi != g)
                 continue;
             JobDesc& jd = r->h_jobs[nj++];
@@ -455,6 +459,7 @@ bool Server::launch_round_locked()
             a.rng_words = b.rng_words;
             a.agg = agg_after_search(b.hot_searched);
             a.rsl_words = rsl_words_for(b.prog.data());
+            a.merged = merged_for(b.prog.data());
             std::memcpy(a.isaac_init, isaac_init, sizeof a.isaac_init);
             set_geometry(a, b.prog.data(), o.precision);
             jd.chunk_begin = groups[g].chunks;
@@ -518,10 +523,10 @@ bool Server::launch_round_locked()
     {
         if (!groups[g].n)
             continue;
-        const int dims = g / 2 + 1, color = g & 1;
+        const int dims = g / 4 + 1, merged = (g >> 1) & 1, color = g & 1;
         const Launchers& L = launchers(o.precision, dims);
         int bps = 0, block = 0;
-        e = L.occ_batch(color, &bps, &block, groups[g].smem);
+        e = L.occ_batch(color, merged, &bps, &block, groups[g].smem);
         if (e != cudaSuccess)
             break;
         if (bps < 1)
@@ -535,7 +540,7 @@ bool Server::launch_round_locked()
         ba.njobs = groups[g].n;
         ba.head = r->d_heads + g;
         ba.order = r->d_order + order_off[g];
-        e = L.batch(ba, color, (int)grid, groups[g].smem, r->stream);
+        e = L.batch(ba, color, merged, (int)grid, groups[g].smem, r->stream);
     }
     if (e == cudaSuccess)
         e = cudaEventRecord(r->done, r->stream);

@@ -407,8 +407,10 @@ __device__ __forceinline__ bool merged_variations(const float* coef, const float
     {
         const float x = t[0], y = t[D - 1];
         float rt = 0.0f, ang = 0.0f;
+        // sqrt(q) as q / sqrt(q) from the reciprocal square root (two
+        // instructions instead of the correctly rounded sequence; a few ulp)
         if (present & (kTaHorseshoe | kTaPolar | kTaJulia))
-            rt = T::sqrt_(q);
+            rt = q > 0.0f ? q * rsqrtf(q) : 0.0f;
         if (present & (kTaPolar | kTaJulia))
             ang = T::atan2_(y, x);
         float X = v[0], Y = v[D - 1];

@@ -22,9 +22,12 @@ The reference converts NaN (an empty cell's 0/0 colour) and values at or
 above 2^bits to an integer pixel, which is undefined behaviour in C++; here
 (as in the GPU kernel) NaN maps to 0 and values saturate at 2^bits - 1.
 
-Parity: the reference's image path needs Boost.GIL and libpng, which are not
-available, so this restatement is not checked against the reference binary
-(parity unpinned); it follows the source lines above.
+Parity: pinned.  The reference's own src/ffr_img.cpp (with ImageRenderer)
+is compiled into oracle/_ref/ffr_img_ref by oracle/build_ref.sh, with
+project-written Boost.GIL / program_options shims and an unencoded image
+writer in place of libpng; tests/golden/make_golden_images.py ran it on
+buffers from the reference's buffer path, and tests/test_image.py checks this
+restatement against those pixels (identical on every case when generated).
 """
 from __future__ import annotations
 
