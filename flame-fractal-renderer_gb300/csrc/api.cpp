@@ -330,7 +330,7 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     int bps = 0, block = 0;
     size_t smem = 0;
     const int color = c->flame.color_dims > 0, spill = c->d_hi != nullptr;
-    const unsigned int pb = (unsigned int)c->prog_host.size();
+    const unsigned int pb = prog_smem_for(c->prog_host.data());
     const int nxf = (int)c->flame.xforms.size();
     int k = kreq;
     if (k != FFR_KERNEL_PLAIN)
@@ -412,7 +412,7 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
 {
     std::memset(&a, 0, sizeof a);
     a.prog = c->d_prog;
-    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.prog_bytes = prog_smem_for(c->prog_host.data());
     a.nxf = (int)c->flame.xforms.size();
     a.color_dims = c->flame.color_dims;
     a.spill = hi != nullptr;
@@ -1317,7 +1317,7 @@ ffr_status ffr_step(ffr_ctx* c, int xf_index, uint64_t key, uint64_t npts,
     StepArgs a;
     std::memset(&a, 0, sizeof a);
     a.prog = c->d_prog;
-    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.prog_bytes = prog_smem_for(c->prog_host.data());
     a.xf_index = xf_index;
     a.key = key;
     a.npts = npts;
@@ -1347,7 +1347,7 @@ ffr_status ffr_trace(ffr_ctx* c, uint64_t key, uint64_t settle, uint64_t n,
     TraceArgs a;
     std::memset(&a, 0, sizeof a);
     a.prog = c->d_prog;
-    a.prog_bytes = (unsigned int)c->prog_host.size();
+    a.prog_bytes = prog_smem_for(c->prog_host.data());
     a.key = key;
     a.settle = settle;
     a.n = n;
@@ -1570,7 +1570,7 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
             size_t sm = 0;
             if ((e = L.occ(g.color, g.merged, rsl_words_for(c->prog_host.data()), hot, &bps,
                            &block,
-                           (unsigned int)c->prog_host.size(),
+                           prog_smem_for(c->prog_host.data()),
                            (int)c->flame.xforms.size(), &sm)) != cudaSuccess)
                 return cfail(e, "occupancy");
             g.smem = std::max(g.smem, sm);

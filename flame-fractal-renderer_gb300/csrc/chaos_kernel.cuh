@@ -39,16 +39,22 @@ struct Prog
     const R* color;
     uint32_t present;       // ProgHeader::tier_a_present
     uint32_t merged;        // ProgHeader::merged
+    const float* fast;      // the compact merged 2-D table, or null
 
-    __device__ __forceinline__ void bind(const unsigned char* base)
+    // sbase: the shared-memory copy of the blob's first h->smem_bytes;
+    // gbase: the whole blob in global memory, for the sections beyond
+    __device__ __forceinline__ void bind(const unsigned char* sbase, const unsigned char* gbase)
     {
-        h = reinterpret_cast<const ProgHeader<R>*>(base);
+        h = reinterpret_cast<const ProgHeader<R>*>(sbase);
         present = h->tier_a_present;
         merged = h->merged;
-        thresh = reinterpret_cast<const uint64_t*>(base + h->off_thresh);
-        xf = reinterpret_cast<const XformT<R>*>(base + h->off_xf);
-        var = reinterpret_cast<const VarT<R>*>(base + h->off_var);
-        color = reinterpret_cast<const R*>(base + h->off_color);
+        const unsigned int lim = h->smem_bytes;
+        auto at = [&](unsigned int off) { return (off < lim ? sbase : gbase) + off; };
+        thresh = reinterpret_cast<const uint64_t*>(at(h->off_thresh));
+        xf = reinterpret_cast<const XformT<R>*>(at(h->off_xf));
+        var = reinterpret_cast<const VarT<R>*>(at(h->off_var));
+        color = reinterpret_cast<const R*>(at(h->off_color));
+        fast = h->off_fast ? reinterpret_cast<const float*>(at(h->off_fast)) : nullptr;
     }
 };
 
@@ -89,6 +95,42 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
     }
 }
 
+// The merged 2-D application from the compact table (flame_program.h): the
+// same operations in the same order as affine<2> + merged_variations +
+// affine<2> on XformT, from five 16-byte loads instead of eight, so the
+// result is the one the general instantiation computes.  False (nothing
+// written, nothing drawn) when merged_variations declines the point.
+template <typename Rng>
+__device__ __forceinline__ bool apply_fast2(const float* f, const float* p, float* out,
+                                            Rng& rng, uint32_t present)
+{
+    const float4 r0 = *reinterpret_cast<const float4*>(f);
+    const float4 r1 = *reinterpret_cast<const float4*>(f + 4);
+    const float4 r2 = *reinterpret_cast<const float4*>(f + 8);
+    float t[2], v[2];
+    {
+        float d = 0.0f;
+        d += r0.x * p[0];
+        d += r0.y * p[1];
+        t[0] = r0.z + d;
+        d = 0.0f;
+        d += r0.w * p[0];
+        d += r1.x * p[1];
+        t[1] = r1.y + d;
+    }
+    if (!merged_variations<2>(f + 12, t, v, rng, present))
+        return false;
+    float d = 0.0f;
+    d += r1.z * v[0];
+    d += r1.w * v[1];
+    out[0] = r2.x + d;
+    d = 0.0f;
+    d += r2.y * v[0];
+    d += r2.z * v[1];
+    out[1] = r2.w + d;
+    return true;
+}
+
 // XForm::applyIteration (xform.hpp:211-227).  For dims < 3 both affines are
 // always applied (identity when absent), for dims >= 3 only when present.
 // MERGED: the instantiation for FP32 programs in the merged form
@@ -97,8 +139,15 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
 // computes exactly what the general instantiation computes for them.
 template <int D, typename R, bool MERGED = false, typename Rng>
 __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& x,
-                                            const R* p, R* out, Rng& rng)
+                                            const R* p, R* out, Rng& rng, int xi = -1)
 {
+    if constexpr (MERGED && D == 2 && sizeof(R) == sizeof(float))
+    {
+        if (pg.fast && xi >= 0 && apply_fast2(pg.fast + xi * kFast2Floats,
+                                              reinterpret_cast<const float*>(p),
+                                              reinterpret_cast<float*>(out), rng, pg.present))
+            return;
+    }
     R t[D], v[D];
     if (D < 3 || x.has_pre)
         affine<D>(x.pre, p, t);
@@ -306,7 +355,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
 {
     using T = RealTraits<R>;
     Prog<R> pg;
-    pg.bind(smem);
+    pg.bind(smem, a.prog);
     const ProgHeader<R>& h = *pg.h;
     const int nxf = a.nxf;
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
@@ -420,7 +469,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     refill_ahead();
                     const int xi = pick_xform<R>(pg, nxf, rng);
                     R q[D];
-                    apply_xform<D, R, MERGED>(pg, pg.xf[xi], p, q, rng);
+                    apply_xform<D, R, MERGED>(pg, pg.xf[xi], p, q, rng, xi);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -438,7 +487,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
-                    apply_xform<D, R, MERGED>(pg, xf, p, q, rng);
+                    apply_xform<D, R, MERGED>(pg, xf, p, q, rng, xi);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -453,7 +502,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 if (h.has_final)
                 {
                     const XformT<R>& ff = pg.xf[nxf];
-                    apply_xform<D, R, MERGED>(pg, ff, p, pf, rng);
+                    apply_xform<D, R, MERGED>(pg, ff, p, pf, rng, nxf);
                     if (COLOR)
                     {
                         if (ff.has_color)
@@ -743,7 +792,7 @@ __global__ void __launch_bounds__(128) step_kernel(const StepArgs a)
     load_program<128>(smem, a.prog, a.prog_bytes);
     __syncthreads();
     Prog<R> pg;
-    pg.bind(smem);
+    pg.bind(smem, a.prog);
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
     DevIsaac<128> rng;
     rng.mem = ismem + threadIdx.x;
@@ -773,7 +822,7 @@ __global__ void trace_kernel(const TraceArgs a)
     load_program<1>(smem, a.prog, a.prog_bytes);
     __syncthreads();
     Prog<R> pg;
-    pg.bind(smem);
+    pg.bind(smem, a.prog);
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
     DevIsaac<1> rng;
     rng.mem = ismem;

@@ -150,7 +150,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
 {
     using Tr = RealTraits<R>;
     Prog<R> pg;
-    pg.bind(smem);
+    pg.bind(smem, a.prog);
     const ProgHeader<R>& h = *pg.h;
     const int nxf = a.nxf;
     const int W = (int)h.rng_words_max;

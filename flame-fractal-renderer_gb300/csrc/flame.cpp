@@ -310,6 +310,37 @@ void pack_xform(const HostXform& h, int dims, XformT<R>& x, int16_t var_begin)
 
 } // namespace
 
+// The FP32 merged form applies (ProgHeader::merged): every variation one of
+// the seven benchmark types, 2-D types only in 2-D flames, and julia at most
+// once per xform (julia's random word differs per instance, so two julias
+// are not one julia of the summed weight; every other type is a fixed map).
+static bool merged_form(const HostFlame& f)
+{
+    static const int32_t kTierA[7] = {V_LINEAR, V_SINUSOIDAL, V_SPHERICAL, V_SWIRL,
+                                      V_HORSESHOE, V_POLAR, V_JULIA};
+    auto ok_xform = [&](const HostXform& x) {
+        int jul = 0;
+        for (const auto& v : x.vars)
+        {
+            bool a = false;
+            for (int k = 0; k < 7; ++k)
+                a = a || v.type == kTierA[k];
+            if (!a)
+                return false;
+            const bool two_d = v.type == V_SWIRL || v.type == V_HORSESHOE
+                || v.type == V_POLAR || v.type == V_JULIA;
+            if (two_d && f.dims != 2)
+                return false;
+            jul += v.type == V_JULIA;
+        }
+        return jul <= 1;
+    };
+    for (const auto& x : f.xforms)
+        if (!ok_xform(x))
+            return false;
+    return !f.has_final || ok_xform(f.final_xf);
+}
+
 template <typename R>
 std::vector<uint8_t> build_program(const HostFlame& f)
 {
@@ -333,12 +364,19 @@ std::vector<uint8_t> build_program(const HostFlame& f)
     size_t off = align16(sizeof(ProgHeader<R>));
     h.off_thresh = (uint32_t)off;
     off = align16(off + sizeof(uint64_t) * nxf);
+    const bool fast2 = sizeof(R) == sizeof(float) && f.dims == 2 && merged_form(f);
+    h.off_fast = fast2 ? (uint32_t)off : 0u;
+    if (fast2)
+        off = align16(off + sizeof(float) * (size_t)(nxf + 1) * kFast2Floats);
+    // shared-memory part: up to here for merged 2-D programs, else all
+    const size_t smem_end = off;
     h.off_xf = (uint32_t)off;
     off = align16(off + sizeof(XformT<R>) * (nxf + 1));
     h.off_var = (uint32_t)off;
     off = align16(off + sizeof(VarT<R>) * nvar);
     h.off_color = (uint32_t)off;
     off = align16(off + sizeof(R) * (size_t)(nxf + 1) * f.color_dims);
+    h.smem_bytes = (uint32_t)(fast2 ? smem_end : off);
     if (off > kMaxProgramBytes || nvar > 32767)
         throw FlameError("flame too large for one device program ("
             + std::to_string(off) + " bytes; limit "
@@ -389,21 +427,7 @@ std::vector<uint8_t> build_program(const HostFlame& f)
     // the xform's summed weight of that type.  Sums of equal terms are the
     // same map (V(t) does not depend on the instance), except julia, whose
     // random word differs per instance.
-    h.merged = 0;
-    if (sizeof(R) == sizeof(float) && !(present & (1u << 7))
-            && (f.dims == 2 || !(present & 0x78u)))
-    {
-        bool ok = true;
-        for (const HostXform* x : all)
-            if (x)
-            {
-                int jul = 0;
-                for (const auto& v : x->vars)
-                    jul += v.type == V_JULIA;
-                ok = ok && jul <= 1;
-            }
-        h.merged = ok ? 1 : 0;
-    }
+    h.merged = sizeof(R) == sizeof(float) && merged_form(f) ? 1 : 0;
     for (int i = 0; i < f.dims; ++i)
     {
         h.size[i] = f.size[i];
@@ -459,6 +483,25 @@ std::vector<uint8_t> build_program(const HostFlame& f)
         }
         for (int c = 0; c < (int)x->color.size(); ++c)
             cp[(size_t)k * f.color_dims + c] = (R)x->color[c];
+        if (fast2)
+        {
+            float* q = reinterpret_cast<float*>(blob.data() + h.off_fast) + (size_t)k * kFast2Floats;
+            const XformT<R>& d = xp[k];
+            // A[i][j] at i * kMaxDims + j, b[i] at kMaxDims * kMaxDims + i
+            const int b0 = kMaxDims * kMaxDims;
+            const R* aff[2] = {d.pre, d.post};
+            for (int a = 0; a < 2; ++a)
+            {
+                q[6 * a + 0] = (float)aff[a][0];
+                q[6 * a + 1] = (float)aff[a][1];
+                q[6 * a + 2] = (float)aff[a][b0];
+                q[6 * a + 3] = (float)aff[a][kMaxDims];
+                q[6 * a + 4] = (float)aff[a][kMaxDims + 1];
+                q[6 * a + 5] = (float)aff[a][b0 + 1];
+            }
+            for (int c = 0; c < 8; ++c)
+                q[12 + c] = (float)d.coef[c];
+        }
     }
     return blob;
 }

@@ -10,6 +10,7 @@
 // Blob layout (all offsets in bytes from the blob start, 16-byte aligned):
 //   ProgHeader<R>
 //   uint64_t thresh[nxf]        xform selection thresholds (see below)
+//   float     fast[(nxf + 1) * kFast2Floats]   merged 2-D FP32 programs only
 //   XformT<R> xf[nxf + 1]       sorted xforms, then the final xform
 //   VarT<R>   var[nvar]         variations of all xforms, in xform order
 //   R         color[(nxf+1) * color_dims]
@@ -56,6 +57,11 @@ struct alignas(16) XformT
     R coef[8];
 };
 
+// compact merged 2-D xform: pre-affine {a00, a01, b0, a10, a11, b1}, then
+// post-affine {a00, a01, b0, a10, a11, b1} (both as XformT stores them),
+// then XformT::coef
+constexpr int kFast2Floats = 20;
+
 template <typename R>
 struct alignas(16) VarT
 {
@@ -95,6 +101,16 @@ struct alignas(16) ProgHeader
     // types, with 2-D types only in 2-D flames and julia at most once per
     // xform.  FP64 programs keep the reference's per-variation order.
     uint32_t merged;
+    // byte offset of the compact table of a merged 2-D program (kFast2Floats
+    // floats per xform, the final xform last), or 0: the two affines and the
+    // merged coefficients in five 16-byte words instead of eight
+    uint32_t off_fast;
+    // the kernels copy the first smem_bytes of the blob into shared memory
+    // and read the rest (sections at offsets at or above it) from the
+    // program's global copy: merged 2-D programs keep only the header, the
+    // thresholds and the compact table in shared memory (their xforms and
+    // variations are read only on rare paths); all others keep everything
+    uint32_t smem_bytes;
     uint32_t pad_;
     uint64_t size[kMaxDims];
     uint64_t mult_i[kMaxDims];

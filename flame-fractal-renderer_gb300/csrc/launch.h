@@ -37,7 +37,7 @@ struct DevStats
 struct RenderArgs
 {
     const unsigned char* prog;      // device copy of the program blob
-    unsigned int prog_bytes;
+    unsigned int prog_bytes;        // its shared-memory part (prog_smem_for)
     int nxf;
     int color_dims;
     int spill;                      // counts may pass 2^32: keep high words
@@ -130,6 +130,18 @@ inline int rsl_words_for(const void* prog)
 }
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
+
+// ProgHeader::smem_bytes of a program blob: the part the kernels copy into
+// shared memory (RenderArgs::prog_bytes)
+inline unsigned int prog_smem_for(const void* prog)
+{
+    static_assert(offsetof(ProgHeader<double>, smem_bytes)
+                  == offsetof(ProgHeader<float>, smem_bytes), "program header layout");
+    uint32_t v = 0;
+    memcpy(&v, static_cast<const unsigned char*>(prog) + offsetof(ProgHeader<double>, smem_bytes),
+           sizeof v);
+    return v;
+}
 
 // ProgHeader::merged of a program blob (0 for FP64 programs)
 inline int merged_for(const void* prog)

@@ -209,7 +209,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     size_t smem = 0;
     if ((e = occ(f.color_dims > 0, merged_for(prog.data()), rsl_words_for(prog.data()), 0,
                  &bps, &block,
-                 (unsigned int)prog.size(), nxf, &smem))
+                 prog_smem_for(prog.data()), nxf, &smem))
             != cudaSuccess)
         return nocuda(e, "occupancy");
     if (bps < 1)
@@ -249,7 +249,7 @@ extern "C" ffr_status ffr_render_noalloc(const char* json, size_t len, const ffr
     RenderArgs a;
     std::memset(&a, 0, sizeof a);
     a.prog = scratch;
-    a.prog_bytes = (unsigned int)prog.size();
+    a.prog_bytes = prog_smem_for(prog.data());
     a.nxf = nxf;
     a.color_dims = f.color_dims;
     a.spill = 0;

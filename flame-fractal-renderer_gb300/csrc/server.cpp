@@ -441,7 +441,7 @@ bool Server::launch_round_locked()
             RenderArgs& a = jd.a;
             std::memset(&jd, 0, sizeof jd);
             a.prog = b.d_prog;
-            a.prog_bytes = (unsigned int)b.prog.size();
+            a.prog_bytes = prog_smem_for(b.prog.data());
             a.nxf = (int)b.flame.xforms.size();
             a.color_dims = b.flame.color_dims;
             a.spill = j->spill;
@@ -671,7 +671,7 @@ void Server::hot_search_locked(SrvBuffer& b, uint64_t sum)
     b.hot_mult = mult;
     b.hot_cells = (int)std::count_if(keys.begin(), keys.end(),
                                      [](unsigned int k) { return k != kHotEmpty; });
-    b.smem_hot = chaos_smem_bytes<kChunkStreams>((unsigned int)b.prog.size(),
+    b.smem_hot = chaos_smem_bytes<kChunkStreams>(prog_smem_for(b.prog.data()),
                                                  (int)b.flame.xforms.size(),
                                                  rsl_words_for(b.prog.data()), true);
 }
@@ -1151,7 +1151,7 @@ ffr_status ffr_server_submit(ffr_server* srv, const char* json, size_t len, cons
         b->init.resize(b->file_bytes() / 8);
         std::memcpy(b->init.data(), init, b->file_bytes());
     }
-    b->smem = chaos_smem_bytes<kChunkStreams>((unsigned int)b->prog.size(),
+    b->smem = chaos_smem_bytes<kChunkStreams>(prog_smem_for(b->prog.data()),
                                               (int)b->flame.xforms.size(),
                                               rsl_words_for(b->prog.data()));
     const uint64_t need = kStagingBytes * kReadSlots + b->prog.size() + b->counts_bytes()
