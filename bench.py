@@ -411,7 +411,7 @@ def run_tetra3d(args):
           tv=tv, clocks=clocks, iterated_per_s=iters / (ms * 1e-3))
 
 
-def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8):
+def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8, scale=1.0):
     """The 256-flame batch (flames.batch_jobs(11)) in one persistent,
     graph-captured launch per step: binned samples/s over `steps` timed
     steps (L2 flushed between them), per-flame TV against FP64 for n_tv
@@ -420,7 +420,8 @@ def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8):
     fl = _flames()
     jobs = fl.batch_jobs(11)
     texts = [json.dumps(f) for f, _ in jobs]
-    ns = [n for _, n in jobs]
+    # scale < 1: the same flames with fewer samples (small profiling cases)
+    ns = [max(1, int(n * scale)) for _, n in jobs]
     rs = [ffr.BufferRenderer(t, precision=ffr.FP32, settle=20, traj_len=4096, device=dev)
           for t in texts]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -469,7 +470,8 @@ def run_batch256(args):
     if got is None:
         return
     ffr, dev = got
-    rec = batch256_record(ffr, dev, args.steps, args.warmup, with_tv=not args.no_tv)
+    rec = batch256_record(ffr, dev, args.steps, args.warmup, with_tv=not args.no_tv,
+                          scale=args.batch_scale)
     _line(args, "256 random 2-D flames (2-8 xforms, 256^2-2048^2, 1e7-1e9 samples) "
           "in one persistent launch", rec["value"], rec["ms_per_step"], "f32",
           {k: rec[k] for k in ("flames", "samples_per_step", "settle", "seed", "traj_len",
@@ -668,6 +670,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--max-active", type=int, default=256)
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="batch256: multiply every flame's sample count (profiling cases)")
     ap.add_argument("--no-sub", action="store_true",
                     help="default workload only: skip the batch and serving sub-records")
     ap.add_argument("--serving-seconds", type=float, default=10.0,

@@ -71,8 +71,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
                   "-I", os.path.join(cuda, "include")]
     jobs = []   # (target, deps, cmd)
     for p in (0, 1):
-        for d in (1, 2, 3):
-            for kind in range(8 if p == 1 else 6):
+        for d in (1, 2, 3, 4):
+            # four dimensions: plain render (kinds 0, 2, 6) and step/trace (5)
+            kinds = range(8 if p == 1 else 6) if d < 4 else ([0, 2, 5, 6] if p == 1 else [0, 2, 5])
+            for kind in kinds:
                 obj = os.path.join(OUT, f"chaos_p{p}_d{d}_k{kind}.o")
                 src = os.path.join(CSRC, "chaos_inst.cu")
                 extra = ["--fmad=false"] if p == 0 else []

@@ -67,7 +67,7 @@ void ffr::set_global_error(const std::string& m)
 
 namespace {
 
-const Launchers kLaunchers[2][3] = {
+const Launchers kLaunchers[2][4] = {
     {
         {launch_render_p0_d1, occupancy_p0_d1, launch_sorted_p0_d1,
          occupancy_sorted_p0_d1, launch_batch_p0_d1, occupancy_batch_p0_d1,
@@ -78,6 +78,8 @@ const Launchers kLaunchers[2][3] = {
         {launch_render_p0_d3, occupancy_p0_d3, launch_sorted_p0_d3,
          occupancy_sorted_p0_d3, launch_batch_p0_d3, occupancy_batch_p0_d3,
          launch_step_p0_d3, launch_trace_p0_d3},
+        {launch_render_p0_d4, occupancy_p0_d4, nullptr, nullptr, nullptr, nullptr,
+         launch_step_p0_d4, launch_trace_p0_d4},
     },
     {
         {launch_render_p1_d1, occupancy_p1_d1, launch_sorted_p1_d1,
@@ -89,6 +91,8 @@ const Launchers kLaunchers[2][3] = {
         {launch_render_p1_d3, occupancy_p1_d3, launch_sorted_p1_d3,
          occupancy_sorted_p1_d3, launch_batch_p1_d3, occupancy_batch_p1_d3,
          launch_step_p1_d3, launch_trace_p1_d3},
+        {launch_render_p1_d4, occupancy_p1_d4, nullptr, nullptr, nullptr, nullptr,
+         launch_step_p1_d4, launch_trace_p1_d4},
     },
 };
 
@@ -126,7 +130,16 @@ struct ffr_ctx
     int tuned_kernel = FFR_KERNEL_PLAIN;
     int tuned_agg = 0;
     bool tuned_hot = false;
+    // resident CTAs per SM the tuned launch uses at most (0: all that fit);
+    // a lower cap runs each thread's streams one after another and never
+    // changes which streams run, so the buffer does not depend on it
+    int tuned_cap = 0;
+    int probe_cap = 0;              // the cap an autotuner probe is planned with
     bool hot_searched = false;      // a hot-cell search ran (probe or autotuner)
+    // shape of the last plan(): CTAs per SM allowed, threads per CTA, streams
+    // each thread runs (reported in ffr_stats)
+    int plan_cap = 0, plan_block = 0;
+    uint64_t plan_spt = 0;
     // hot-cell table of the plain kernel (kHotSlots keys), installed by the
     // autotuner; hot_mult 0 = none
     unsigned int* d_hot = nullptr;
@@ -333,6 +346,14 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     const unsigned int pb = prog_smem_for(c->prog_host.data());
     const int nxf = (int)c->flame.xforms.size();
     int k = kreq;
+    if (k != FFR_KERNEL_PLAIN && !c->L().occ_sorted)
+    {
+        // no xform-sorted instantiation for this dimension count
+        if (k == FFR_KERNEL_SORTED)
+            return fail(c, FFR_ERR_ARG, "xform-sorted kernel cannot run this flame "
+                "(dims " + std::to_string(c->flame.dims) + ": plain kernel only)");
+        k = FFR_KERNEL_PLAIN;
+    }
     if (k != FFR_KERNEL_PLAIN)
     {
         CU(c, c->L().occ_sorted(color, spill, &bps, &block, pb, nxf, program_words(c), &smem));
@@ -355,13 +376,16 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
             "(program " + std::to_string(c->prog_host.size()) + " bytes)");
     const uint64_t resident = (uint64_t)c->sm_count * bps * block;
     uint64_t S = c->opts.streams ? c->opts.streams : resident;
+    // the autotuner's cap on resident CTAs per SM (streams stay as above)
+    int cap = c->probe_cap ? c->probe_cap : (c->tuned ? c->tuned_cap : 0);
+    cap = cap > 0 && cap < bps ? cap : bps;
     uint64_t len = c->opts.traj_len;
     if (len == 0)
         len = samples ? std::max<uint64_t>(1, (samples + S - 1) / S) : 1;
     const uint64_t ntraj = samples ? (samples + len - 1) / len : 0;
     const uint64_t active = std::min<uint64_t>(S, ntraj);
     uint64_t blocks = (active + block - 1) / block;
-    blocks = std::min<uint64_t>(blocks, (uint64_t)c->sm_count * bps);
+    blocks = std::min<uint64_t>(blocks, (uint64_t)c->sm_count * cap);
     if (blocks < 1)
         blocks = 1;
     // per-thread xform counters are u32: bound one thread's samples
@@ -376,6 +400,9 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     *streams = S;
     *L = len;
     *grid = (int)blocks;
+    c->plan_cap = cap;
+    c->plan_block = block;
+    c->plan_spt = streams_per_thread;
     if (hot)
         *hot = use_hot && c->hot_mult != 0;
     return FFR_OK;
@@ -513,6 +540,7 @@ struct TuneChoice
 {
     int kernel = FFR_KERNEL_PLAIN;
     int agg = 0;
+    int cap = 0;                            // resident CTAs per SM (0: all that fit)
     unsigned int hot_mult = 0;              // 0: no hot-cell table
     std::vector<unsigned int> hot_keys;     // kHotSlots keys when hot_mult != 0
 };
@@ -668,6 +696,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
             c->tuned_spill = spill;
             c->tuned_kernel = *kernel = ch.kernel;
             c->tuned_agg = *agg = ch.agg;
+            c->tuned_cap = ch.cap;
             c->tuned_hot = *hot = ch.hot_mult != 0;
             c->hot_searched = true;
             return FFR_OK;
@@ -765,6 +794,34 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         for (int g : {0, 1})
             if (st == FFR_OK)
                 st = probe(FFR_KERNEL_PLAIN, g, true);
+    // launch shape for the best candidate: fewer resident CTAs per SM, each
+    // thread then running more streams one after another (the streams, and
+    // so the buffer, stay the same); kept only when 3% faster
+    int best_cap = 0;
+    if (st == FFR_OK)
+    {
+        uint64_t S0 = 0, L0 = 0;
+        int g0 = 0, k0 = 0;
+        bool h0 = best_h;
+        c->probe_cap = 0;
+        if (plan(c, P, best_k, &S0, &L0, &g0, &k0, &h0) == FFR_OK)
+        {
+            const int full = c->plan_cap;
+            for (int cap : {full - 1, (full + 1) / 2})
+            {
+                if (cap < 1 || cap >= full || st != FFR_OK)
+                    continue;
+                c->probe_cap = cap;
+                const float prev = best;
+                st = probe(best_k, best_a, best_h);
+                if (best < 0.97f * prev)
+                    best_cap = cap;
+                else
+                    best = prev;
+            }
+        }
+        c->probe_cap = 0;
+    }
     cudaFree(buf);
     if (st != FFR_OK)
         return st;
@@ -779,6 +836,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     c->tuned_kernel = *kernel = best_k;
     c->tuned_agg = *agg = best_a;
     c->tuned_hot = *hot = best_h;
+    c->tuned_cap = best_cap;
     // the table (or its absence) is the autotuner's decision: batches reuse it
     c->hot_searched = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -787,6 +845,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     TuneChoice ch;
     ch.kernel = best_k;
     ch.agg = best_a;
+    ch.cap = best_cap;
     ch.hot_mult = mult;
     ch.hot_keys = std::move(keys);
     g_tune_cache[tune_key(c)] = std::move(ch);
@@ -1122,6 +1181,10 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
         st->agg = agg;
         st->hot_cells = hot ? c->hot_cells : 0;
         st->aux_launches = (int32_t)c->aux_launches;
+        st->ctas = (uint64_t)grid;
+        st->streams_per_thread = c->plan_spt;
+        st->ctas_per_sm = c->plan_cap;
+        st->threads_per_cta = c->plan_block;
     }
     if (hs.cancelled)
         return fail(c, FFR_ERR_TIMEOUT, "render cancelled");
@@ -1497,6 +1560,10 @@ ffr_status ffr_batch_create(ffr_ctx* const* ctxs, size_t n, ffr_batch** out)
 {
     if (!out || !ctxs || n == 0)
         return fail(nullptr, FFR_ERR_ARG, "ffr_batch_create: no contexts");
+    for (size_t i = 0; i < n; ++i)
+        if (ctxs[i] && ctxs[i]->flame.dims > 3)
+            return fail(nullptr, FFR_ERR_ARG, "ffr_batch_create: batched renders take "
+                        "1- to 3-dimensional flames (render 4-D flames with ffr_render)");
     *out = nullptr;
     const int dev = ctxs[0]->device, prec = ctxs[0]->opts.precision;
     for (size_t i = 0; i < n; ++i)

@@ -29,7 +29,10 @@
 
 namespace ffr {
 
-constexpr int kMaxDims = 3;          // ffr-buf compiles dims 1..3 (ffr_buf.cpp:134-141)
+// dims 1..4: the reference's templates are generic over dims, its ffr-buf
+// CLI compiles 1..3 (ffr_buf.cpp:134-141); 4 is rendered by ffr_render
+// (plain kernel) here
+constexpr int kMaxDims = 4;
 constexpr int kMaxColorDims = 127;   // flame.hpp:156
 constexpr int kVarParams = 16;
 constexpr int kMaxXformIds = 4096;

@@ -346,6 +346,10 @@ FFR_DECLARE_LAUNCHERS(0, 3)
 FFR_DECLARE_LAUNCHERS(1, 1)
 FFR_DECLARE_LAUNCHERS(1, 2)
 FFR_DECLARE_LAUNCHERS(1, 3)
+// four dimensions: plain render, step and trace kernels only (no sorted or
+// batch instantiation; the Launchers entries for those are null)
+FFR_DECLARE_LAUNCHERS(0, 4)
+FFR_DECLARE_LAUNCHERS(1, 4)
 
 typedef cudaError_t (*RenderFn)(const RenderArgs&, int, cudaStream_t);
 typedef cudaError_t (*OccFn)(int, int, int, int, int*, int*, unsigned int, int, size_t*);

@@ -112,12 +112,12 @@ ffr_status device_buffer(const void* p, int device, const char* name)
 
 void pick_launchers(int precision, int dims, RenderFn* r, OccFn* o)
 {
-    static const RenderFn rf[2][3] = {
-        {launch_render_p0_d1, launch_render_p0_d2, launch_render_p0_d3},
-        {launch_render_p1_d1, launch_render_p1_d2, launch_render_p1_d3}};
-    static const OccFn of[2][3] = {
-        {occupancy_p0_d1, occupancy_p0_d2, occupancy_p0_d3},
-        {occupancy_p1_d1, occupancy_p1_d2, occupancy_p1_d3}};
+    static const RenderFn rf[2][4] = {
+        {launch_render_p0_d1, launch_render_p0_d2, launch_render_p0_d3, launch_render_p0_d4},
+        {launch_render_p1_d1, launch_render_p1_d2, launch_render_p1_d3, launch_render_p1_d4}};
+    static const OccFn of[2][4] = {
+        {occupancy_p0_d1, occupancy_p0_d2, occupancy_p0_d3, occupancy_p0_d4},
+        {occupancy_p1_d1, occupancy_p1_d2, occupancy_p1_d3, occupancy_p1_d4}};
     *r = rf[precision][dims - 1];
     *o = of[precision][dims - 1];
 }

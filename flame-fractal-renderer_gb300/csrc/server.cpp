@@ -1140,6 +1140,9 @@ ffr_status ffr_server_submit(ffr_server* srv, const char* json, size_t len, cons
     }
     if (b->flame.xforms.size() > (size_t)kMaxXformIds)
         return sfail(s, FFR_ERR_ARG, "too many xforms");
+    if (b->flame.dims > 3)
+        return sfail(s, FFR_ERR_ARG, "the serving loop renders 1- to 3-dimensional flames "
+                                     "(render 4-D flames with ffr_render)");
     {
         const ProgHeader<double>* h = reinterpret_cast<const ProgHeader<double>*>(b->prog.data());
         b->rng_words = (int)h->rng_words_max;   // same offset in the float header

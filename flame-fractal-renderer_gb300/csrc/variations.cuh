@@ -173,11 +173,34 @@ __device__ __forceinline__ R rand_gauss(Rng& rng)
     return r * c;
 }
 
-// FlameRNG::randDirection<dims> (flame_rng.hpp:171-217)
+// FlameRNG::randDirection<dims> (flame_rng.hpp:171-217); above 3 dims a
+// vector of gaussian pairs (randGaussianPair, the last pair's second value
+// unused for odd dims) divided by its norm, Point / k being multiplication
+// by 1 / k (point.hpp:135-139)
 template <int D, typename R, typename Rng>
 __device__ __forceinline__ void rand_dir(Rng& rng, R* d)
 {
     using T = RealTraits<R>;
+    if (D > 3)
+    {
+#pragma unroll
+        for (int i = 0; i < D; i += 2)
+        {
+            const R u1 = T::unit(rng.next());
+            const R u2 = (R(2) * T::pi) * T::unit(rng.next());
+            const R r = T::sqrt_(R(-2) * T::log_(u1));
+            R s, c;
+            T::sincos_(u2, &s, &c);
+            d[i] = r * c;
+            if (i + 1 < D)
+                d[i + 1] = r * s;
+        }
+        const R k = R(1) / n2<D>(d);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            d[i] *= k;
+        return;
+    }
     if (D == 1)
     {
         d[0] = T::copysign_(R(1), T::unit(rng.next()) - R(0.5));

@@ -50,7 +50,9 @@ int find_name(const std::string& n, int first, int last)
 // 1-D and 2-D, 2 in 3-D) summed over the class's calc()
 uint32_t variation_rng_words(int id, int dims)
 {
-    const uint32_t dw = dims == 3 ? 2 : 1;
+    // randDirection<dims>: 1 word for dims 1 and 2, 2 for 3, a gaussian
+    // pair (2 words) per two coordinates above 3 (flame_rng.hpp:171-217)
+    const uint32_t dw = dims == 3 ? 2 : (dims > 3 ? 2 * (uint32_t)((dims + 1) / 2) : 1);
     switch (id)
     {
     case V_NOISE: case V_BLUR: return 1 + dw;

@@ -20,8 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libffr_gpu.so")
 CLI_PATH = os.path.join(HERE, "_build", "ffr-buf")
 
-FFR_ABI_VERSION = 2
-MAX_DIMS = 3
+FFR_ABI_VERSION = 3
+MAX_DIMS = 4
 MAX_XFORM_IDS = 4096
 MAX_BAD_RECORDS = 4096
 
@@ -82,7 +82,9 @@ class Stats(ctypes.Structure):
                 ("streams", ctypes.c_uint64), ("traj_len", ctypes.c_uint64),
                 ("settle", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
                 ("kernel", ctypes.c_int32), ("agg", ctypes.c_int32),
-                ("hot_cells", ctypes.c_int32), ("aux_launches", ctypes.c_int32)]
+                ("hot_cells", ctypes.c_int32), ("aux_launches", ctypes.c_int32),
+                ("ctas", ctypes.c_uint64), ("streams_per_thread", ctypes.c_uint64),
+                ("ctas_per_sm", ctypes.c_int32), ("threads_per_cta", ctypes.c_int32)]
 
 
 class ImageInfo(ctypes.Structure):
@@ -216,6 +218,10 @@ class RenderStats:
     agg: int
     hot_cells: int = 0
     aux_launches: int = 0
+    ctas: int = 0
+    streams_per_thread: int = 0
+    ctas_per_sm: int = 0
+    threads_per_cta: int = 0
 
     @property
     def ok(self) -> bool:
@@ -234,7 +240,8 @@ def _render_stats(status: int, st: Stats, n: int) -> RenderStats:
         bad_pts=np.array([[st.bad_pts[k][i] for i in range(n)] for k in range(nrec)]).reshape(nrec, n),
         streams=st.streams, traj_len=st.traj_len, settle=st.settle,
         kernel_ms=st.kernel_ms, kernel=st.kernel, agg=st.agg, hot_cells=st.hot_cells,
-        aux_launches=st.aux_launches)
+        aux_launches=st.aux_launches, ctas=st.ctas, streams_per_thread=st.streams_per_thread,
+        ctas_per_sm=st.ctas_per_sm, threads_per_cta=st.threads_per_cta)
 
 
 def isaac_words(key: int, n: int, device: int = 0) -> np.ndarray:

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FFR_ABI_VERSION 2
+#define FFR_ABI_VERSION 3
 
 typedef enum ffr_status {
     FFR_OK = 0,
@@ -78,7 +78,11 @@ typedef struct ffr_opts {
     uint64_t timeout_ms;
 } ffr_opts;
 
-#define FFR_MAX_DIMS 3
+/* dimensions 1..4: ffr-buf's 1..3 (ffr_buf.cpp:134-141) and 4, which the
+   reference's BufferRenderer<dims> template also renders; 4-D flames run
+   through ffr_render / ffr_render_noalloc (plain kernel), not batches or the
+   serving loop */
+#define FFR_MAX_DIMS 4
 #define FFR_MAX_XFORM_IDS 4096
 #define FFR_MAX_BAD_RECORDS 4096
 
@@ -116,6 +120,14 @@ typedef struct ffr_stats {
     int32_t aux_launches;        /* kernels this call launched besides the
                                     render kernel: count-bound reductions,
                                     autotuner probes, hot-cell search */
+    /* launch shape: CTAs of threads_per_cta threads, at most ctas_per_sm
+       resident per SM (the autotuner may cap it below what fits), each
+       thread running streams_per_thread streams one after the other (the
+       reference's trajectories per thread, buffer_renderer.hpp:296-334) */
+    uint64_t ctas;
+    uint64_t streams_per_thread;
+    int32_t ctas_per_sm;
+    int32_t threads_per_cta;
 } ffr_stats;
 
 typedef struct ffr_ctx ffr_ctx;

@@ -176,9 +176,37 @@ static inline double rand_gauss(isaac_t *s)
     return r * cs;
 }
 
-/* FlameRNG::randDirection<dims> (flame_rng.hpp:171-217) */
+/* FlameRNG::randGaussianPair (flame_rng.hpp:115-140), both values */
+static inline void rand_gauss_pair(isaac_t *s, double *z1, double *z2)
+{
+    double u1 = rand_num(s);
+    double u2 = (2.0 * M_PI) * rand_num(s);
+    double r = sqrt(-2.0 * log(u1));
+    double sn, cs;
+    sincos(u2, &sn, &cs);
+    *z1 = r * cs;
+    *z2 = r * sn;
+}
+
+/* FlameRNG::randDirection<dims> (flame_rng.hpp:171-217); above 3 dims a
+   vector of gaussian pairs (the last one's second value unused for odd
+   dims) divided by its norm, Point / k being multiplication by 1 / k */
 static inline void rand_dir(isaac_t *s, int dims, double *d)
 {
+    if (dims > 3) {
+        double unused, n2 = 0.0, k;
+        int i;
+        for (i = 0; i + 1 < dims; i += 2)
+            rand_gauss_pair(s, &d[i], &d[i + 1]);
+        if (dims % 2)
+            rand_gauss_pair(s, &d[dims - 1], &unused);
+        for (i = 0; i < dims; ++i)
+            n2 += d[i] * d[i];
+        k = 1.0 / sqrt(n2);
+        for (i = 0; i < dims; ++i)
+            d[i] *= k;
+        return;
+    }
     if (dims == 1) {
         d[0] = copysign(1.0, rand_num(s) - 0.5);
     } else if (dims == 2) {
@@ -202,7 +230,9 @@ static inline void rand_dir(isaac_t *s, int dims, double *d)
 /* RNG words one call of each variation draws (fixed per variation) */
 int oracle_variation_words(int type, int dims)
 {
-    int dw = dims == 3 ? 2 : 1;
+    /* randDirection<dims> draws: 1 (dims 1, 2), 2 (dims 3), 2 per gaussian
+       pair above 3 dims */
+    int dw = dims == 3 ? 2 : (dims > 3 ? 2 * ((dims + 1) / 2) : 1);
     switch (type) {
     case OR_V_NOISE: case OR_V_BLUR: return 1 + dw;
     case OR_V_GAUSSIAN_BLUR: case OR_V_PRE_BLUR: return 2 + dw;

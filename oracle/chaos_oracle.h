@@ -8,7 +8,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
-#define OR_MAXD 3          /* dimensions compiled into ffr-buf: 1, 2, 3 */
+#define OR_MAXD 4          /* dimensions 1..4 (ffr-buf compiles 1..3; BufferRenderer<4> for 4) */
 #define OR_MAXC 128        /* color_dimensions <= 127 (flame.hpp:156) */
 #define OR_MAXX 4096       /* xform ids reported in or_stats */
 #define OR_NPARAM 16

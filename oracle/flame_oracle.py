@@ -41,7 +41,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 
-MAXD = 3
+MAXD = 4
 MAXC = 128
 MAXX = 4096
 NPARAM = 16
@@ -94,7 +94,7 @@ def _cos(x):
 
 def rng_words(name: str, dims: int) -> int:
     """RNG words one call draws (FlameRNG draw counts, flame_rng.hpp)."""
-    dw = 2 if dims == 3 else 1
+    dw = 2 if dims == 3 else (2 * ((dims + 1) // 2) if dims > 3 else 1)
     if name in ("noise", "blur"):
         return 1 + dw
     if name in ("gaussian_blur", "pre_blur"):

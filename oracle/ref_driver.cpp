@@ -463,6 +463,9 @@ static int by_dims(const Json& j, A... a)
     case 1: return F<1>::run(j, a...);
     case 2: return F<2>::run(j, a...);
     case 3: return F<3>::run(j, a...);
+    // the reference's templates are generic over dims; its ffr-buf CLI
+    // instantiates 1..3 only (ffr_buf.cpp:134-141)
+    case 4: return F<4>::run(j, a...);
     default:
         std::fprintf(stderr, "ERROR: %lldD not supported\n", (long long)d);
         return 1;
