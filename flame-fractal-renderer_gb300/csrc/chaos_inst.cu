@@ -8,7 +8,8 @@
 //   4  persistent batch kernel with colour
 //   5  single-step and trace kernels
 //   6  FP32 only: plain render kernels for merged-form programs (both colour
-//      variants; ProgHeader::merged, only the seven benchmark variations)
+//      variants, variation sets 1 and 2; ProgHeader::merged, only the seven
+//      benchmark variations)
 //   7  FP32 only: persistent batch kernels for merged-form programs
 // Each general render kernel inlines every variation, so one kernel per
 // object keeps the slowest object (FP64 without contraction) short.  The FP64 objects are
@@ -42,22 +43,23 @@ cudaError_t FFR_NAME(launch_batch_color)(const BatchArgs& b, int grid, size_t sm
 cudaError_t FFR_NAME(occupancy_batch_color)(int* blocks_per_sm, size_t smem);
 // the merged-form instantiations (FP32, kinds 6 and 7)
 cudaError_t FFR_NAME(launch_render_merged)(const RenderArgs& a, int grid, cudaStream_t st);
-cudaError_t FFR_NAME(occupancy_merged)(int color, int rsl_words, int hot, int* blocks_per_sm,
-                                       unsigned int prog_bytes, int nxf, size_t* smem);
-cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int grid, size_t smem,
-                                          cudaStream_t st);
-cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int* blocks_per_sm, size_t smem);
+cudaError_t FFR_NAME(occupancy_merged)(int color, int vs, int rsl_words, int hot,
+                                       int* blocks_per_sm, unsigned int prog_bytes, int nxf,
+                                       size_t* smem);
+cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int vs, int grid,
+                                          size_t smem, cudaStream_t st);
+cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int vs, int* blocks_per_sm, size_t smem);
 
 constexpr int kBlock = 128;
 
 #if FFR_KIND == 0 || FFR_KIND == 2 || FFR_KIND == 6
 
-template <bool C, bool M = false>
+template <bool C, int V = 0>
 static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(a.prog_bytes, a.nxf, a.rsl_words,
                                                  a.hot_keys != nullptr);
-    auto k = chaos_kernel<FFR_D, Real, C, kBlock, M>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock, V>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -66,12 +68,12 @@ static cudaError_t launch_one(const RenderArgs& a, int grid, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <bool C, bool M = false>
+template <bool C, int V = 0>
 static cudaError_t occ_one(int* bps, unsigned int prog_bytes, int nxf, int rsl_words, int hot,
                            size_t* smem_out)
 {
     const size_t smem = chaos_smem_bytes<kBlock>(prog_bytes, nxf, rsl_words, hot != 0);
-    auto k = chaos_kernel<FFR_D, Real, C, kBlock, M>;
+    auto k = chaos_kernel<FFR_D, Real, C, kBlock, V>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess)
@@ -101,8 +103,8 @@ cudaError_t FFR_NAME(occupancy)(int color, int merged, int rsl_words, int hot,
     *block = kBlock;
 #if FFR_P == 1
     if (merged)
-        return FFR_NAME(occupancy_merged)(color, rsl_words, hot, blocks_per_sm, prog_bytes, nxf,
-                                          smem);
+        return FFR_NAME(occupancy_merged)(color, merged, rsl_words, hot, blocks_per_sm,
+                                          prog_bytes, nxf, smem);
 #else
     (void)merged;
 #endif
@@ -127,43 +129,50 @@ cudaError_t FFR_NAME(occupancy_color)(int rsl_words, int hot, int* blocks_per_sm
 
 cudaError_t FFR_NAME(launch_render_merged)(const RenderArgs& a, int grid, cudaStream_t st)
 {
-    return a.color_dims > 0 ? launch_one<true, true>(a, grid, st)
-                            : launch_one<false, true>(a, grid, st);
+    if (a.merged == 2)
+        return a.color_dims > 0 ? launch_one<true, 2>(a, grid, st)
+                                : launch_one<false, 2>(a, grid, st);
+    return a.color_dims > 0 ? launch_one<true, 1>(a, grid, st)
+                            : launch_one<false, 1>(a, grid, st);
 }
 
-cudaError_t FFR_NAME(occupancy_merged)(int color, int rsl_words, int hot, int* blocks_per_sm,
-                                       unsigned int prog_bytes, int nxf, size_t* smem)
+cudaError_t FFR_NAME(occupancy_merged)(int color, int vs, int rsl_words, int hot,
+                                       int* blocks_per_sm, unsigned int prog_bytes, int nxf,
+                                       size_t* smem)
 {
-    return color ? occ_one<true, true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
-                 : occ_one<false, true>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
+    if (vs == 2)
+        return color ? occ_one<true, 2>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
+                     : occ_one<false, 2>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
+    return color ? occ_one<true, 1>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem)
+                 : occ_one<false, 1>(blocks_per_sm, prog_bytes, nxf, rsl_words, hot, smem);
 }
 
 #endif
 
 #if FFR_KIND == 3 || FFR_KIND == 4 || FFR_KIND == 7
 
-template <bool C, bool M = false>
+template <bool C, int V = 0>
 static cudaError_t batch_attr(size_t smem)
 {
-    return cudaFuncSetAttribute(chaos_batch_kernel<FFR_D, Real, C, kBlock, M>,
+    return cudaFuncSetAttribute(chaos_batch_kernel<FFR_D, Real, C, kBlock, V>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <bool C, bool M = false>
+template <bool C, int V = 0>
 static cudaError_t batch_launch(const BatchArgs& b, int grid, size_t smem, cudaStream_t st)
 {
-    chaos_batch_kernel<FFR_D, Real, C, kBlock, M><<<grid, kBlock, smem, st>>>(b);
+    chaos_batch_kernel<FFR_D, Real, C, kBlock, V><<<grid, kBlock, smem, st>>>(b);
     return cudaGetLastError();
 }
 
-template <bool C, bool M = false>
+template <bool C, int V = 0>
 static cudaError_t batch_occ(int* blocks_per_sm, size_t smem)
 {
-    cudaError_t e = batch_attr<C, M>(smem);
+    cudaError_t e = batch_attr<C, V>(smem);
     if (e != cudaSuccess)
         return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        blocks_per_sm, chaos_batch_kernel<FFR_D, Real, C, kBlock, M>, kBlock, smem);
+        blocks_per_sm, chaos_batch_kernel<FFR_D, Real, C, kBlock, V>, kBlock, smem);
 }
 
 #if FFR_KIND == 3
@@ -173,7 +182,7 @@ cudaError_t FFR_NAME(launch_batch)(const BatchArgs& b, int color, int merged, in
 {
 #if FFR_P == 1
     if (merged)
-        return FFR_NAME(launch_batch_merged)(b, color, grid, smem, st);
+        return FFR_NAME(launch_batch_merged)(b, color, merged, grid, smem, st);
 #else
     (void)merged;
 #endif
@@ -187,7 +196,7 @@ cudaError_t FFR_NAME(occupancy_batch)(int color, int merged, int* blocks_per_sm,
     *block = kBlock;
 #if FFR_P == 1
     if (merged)
-        return FFR_NAME(occupancy_batch_merged)(color, blocks_per_sm, smem);
+        return FFR_NAME(occupancy_batch_merged)(color, merged, blocks_per_sm, smem);
 #else
     (void)merged;
 #endif
@@ -198,17 +207,23 @@ cudaError_t FFR_NAME(occupancy_batch)(int color, int merged, int* blocks_per_sm,
 #elif FFR_KIND == 7
 
 #if FFR_P == 1
-cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int grid, size_t smem,
-                                          cudaStream_t st)
+cudaError_t FFR_NAME(launch_batch_merged)(const BatchArgs& b, int color, int vs, int grid,
+                                          size_t smem, cudaStream_t st)
 {
-    return color ? batch_launch<true, true>(b, grid, smem, st)
-                 : batch_launch<false, true>(b, grid, smem, st);
+    if (vs == 2)
+        return color ? batch_launch<true, 2>(b, grid, smem, st)
+                     : batch_launch<false, 2>(b, grid, smem, st);
+    return color ? batch_launch<true, 1>(b, grid, smem, st)
+                 : batch_launch<false, 1>(b, grid, smem, st);
 }
 
-cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int* blocks_per_sm, size_t smem)
+cudaError_t FFR_NAME(occupancy_batch_merged)(int color, int vs, int* blocks_per_sm, size_t smem)
 {
-    return color ? batch_occ<true, true>(blocks_per_sm, smem)
-                 : batch_occ<false, true>(blocks_per_sm, smem);
+    if (vs == 2)
+        return color ? batch_occ<true, 2>(blocks_per_sm, smem)
+                     : batch_occ<false, 2>(blocks_per_sm, smem);
+    return color ? batch_occ<true, 1>(blocks_per_sm, smem)
+                 : batch_occ<false, 1>(blocks_per_sm, smem);
 }
 #endif
 

@@ -100,9 +100,9 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
 // affine<2> on XformT, from five 16-byte loads instead of eight, so the
 // result is the one the general instantiation computes.  False (nothing
 // written, nothing drawn) when merged_variations declines the point.
-template <typename Rng>
+template <bool ALL, typename Rng>
 __device__ __forceinline__ bool apply_fast2(const float* f, const float* p, float* out,
-                                            Rng& rng, uint32_t present)
+                                            Rng& rng, uint32_t present, bool carry)
 {
     const float4 r0 = *reinterpret_cast<const float4*>(f);
     const float4 r1 = *reinterpret_cast<const float4*>(f + 4);
@@ -118,7 +118,7 @@ __device__ __forceinline__ bool apply_fast2(const float* f, const float* p, floa
         d += r1.x * p[1];
         t[1] = r1.y + d;
     }
-    if (!merged_variations<2>(f + 12, t, v, rng, present))
+    if (!merged_variations<2, ALL>(f + 12, t, v, rng, present, carry))
         return false;
     float d = 0.0f;
     d += r1.z * v[0];
@@ -133,19 +133,25 @@ __device__ __forceinline__ bool apply_fast2(const float* f, const float* p, floa
 
 // XForm::applyIteration (xform.hpp:211-227).  For dims < 3 both affines are
 // always applied (identity when absent), for dims >= 3 only when present.
-// MERGED: the instantiation for FP32 programs in the merged form
-// (ProgHeader::merged), which contain only the seven benchmark types; it
-// carries no code for the other 91 (smaller kernels, no stack frame) and
-// computes exactly what the general instantiation computes for them.
-template <int D, typename R, bool MERGED = false, typename Rng>
+// VS (variation set): 0 = the general instantiation; 1 and 2 = the
+// instantiations for FP32 programs in the merged form (ProgHeader::merged),
+// which contain only the seven benchmark types: they carry no code for the
+// other 91 (smaller kernels, no stack frame) and compute exactly what the
+// general instantiation computes for them; 2 evaluates all seven types
+// without per-type branches (merged_variations ALL).  carry: julia's word
+// is taken without a branch (the ISAAC carry area is in use).
+template <int D, typename R, int VS = 0, typename Rng>
 __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& x,
-                                            const R* p, R* out, Rng& rng, int xi = -1)
+                                            const R* p, R* out, Rng& rng, int xi = -1,
+                                            bool carry = false)
 {
+    constexpr bool MERGED = VS != 0;
     if constexpr (MERGED && D == 2 && sizeof(R) == sizeof(float))
     {
-        if (pg.fast && xi >= 0 && apply_fast2(pg.fast + xi * kFast2Floats,
-                                              reinterpret_cast<const float*>(p),
-                                              reinterpret_cast<float*>(out), rng, pg.present))
+        if (pg.fast && xi >= 0 && apply_fast2<VS == 2>(pg.fast + xi * kFast2Floats,
+                                                       reinterpret_cast<const float*>(p),
+                                                       reinterpret_cast<float*>(out), rng,
+                                                       pg.present, carry))
             return;
     }
     R t[D], v[D];
@@ -348,7 +354,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi, unsi
 
 // Runs streams s_first, s_first + s_stride, ... (below the job's active
 // stream count), then merges this CTA's statistics into a.stats.
-template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
+template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
 __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem,
                                            unsigned long long s_first,
                                            unsigned long long s_stride)
@@ -360,6 +366,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     const int nxf = a.nxf;
     uint64_t* ismem = reinterpret_cast<uint64_t*>(smem + align16u(a.prog_bytes));
     const int rsl_words = a.rsl_words;
+    // refill ahead keeps every word of a step in the result array
+    const bool carry = rsl_words > 16;
     uint32_t* xfc_local = reinterpret_cast<uint32_t*>(ismem + (16 + rsl_words) * BLOCK);
     unsigned long long* xfc_shared = reinterpret_cast<unsigned long long*>(xfc_local);
     const bool packed_xfc = nxf <= kPackedXfCounters;
@@ -469,7 +477,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     refill_ahead();
                     const int xi = pick_xform<R>(pg, nxf, rng);
                     R q[D];
-                    apply_xform<D, R, MERGED>(pg, pg.xf[xi], p, q, rng, xi);
+                    apply_xform<D, R, VS>(pg, pg.xf[xi], p, q, rng, xi, carry);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -487,7 +495,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
-                    apply_xform<D, R, MERGED>(pg, xf, p, q, rng, xi);
+                    apply_xform<D, R, VS>(pg, xf, p, q, rng, xi, carry);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -502,7 +510,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 if (h.has_final)
                 {
                     const XformT<R>& ff = pg.xf[nxf];
-                    apply_xform<D, R, MERGED>(pg, ff, p, pf, rng, nxf);
+                    apply_xform<D, R, VS>(pg, ff, p, pf, rng, nxf, carry);
                     if (COLOR)
                     {
                         if (ff.has_color)
@@ -721,13 +729,13 @@ __host__ __device__ constexpr int render_min_blocks()
     return sizeof(R) == 4 ? 6 : 4;
 }
 
-template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
+template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
 __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
     __syncthreads();
-    chaos_body<D, R, COLOR, BLOCK, MERGED>(a, smem,
+    chaos_body<D, R, COLOR, BLOCK, VS>(a, smem,
                                            (unsigned long long)blockIdx.x * BLOCK + threadIdx.x,
                                            (unsigned long long)gridDim.x * BLOCK);
 }
@@ -739,7 +747,7 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(co
 // so every job's buffer is the same alone and in the batch.  The claimed
 // job's arguments are copied to shared memory and its program is reloaded
 // only when the CTA moves to another job.
-template <int D, typename R, bool COLOR, int BLOCK, bool MERGED = false>
+template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
 __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_kernel(const BatchArgs b)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -777,7 +785,7 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_ker
             __syncthreads();
             cur = j;
         }
-        chaos_body<D, R, COLOR, BLOCK, MERGED>(s_args, smem, s_chunk * BLOCK + threadIdx.x,
+        chaos_body<D, R, COLOR, BLOCK, VS>(s_args, smem, s_chunk * BLOCK + threadIdx.x,
                                                ~0ull >> 1);
         __syncthreads();
     }

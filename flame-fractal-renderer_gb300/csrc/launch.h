@@ -143,15 +143,29 @@ inline unsigned int prog_smem_for(const void* prog)
     return v;
 }
 
-// ProgHeader::merged of a program blob (0 for FP64 programs)
+// The kernel variation set for a program blob (RenderArgs::merged): 0 =
+// general (FP64 programs, and FP32 ones outside the merged form); 1 = the
+// merged-form instantiation with a branch per type the flame uses; 2 = the
+// merged-form instantiation evaluating all seven types without branches, for
+// 2-D flames that use at least five of them
 inline int merged_for(const void* prog)
 {
     static_assert(offsetof(ProgHeader<double>, merged) == offsetof(ProgHeader<float>, merged),
                   "program header layout");
-    uint32_t v = 0;
-    memcpy(&v, static_cast<const unsigned char*>(prog) + offsetof(ProgHeader<double>, merged),
-           sizeof v);
-    return v ? 1 : 0;
+    static_assert(offsetof(ProgHeader<double>, tier_a_present)
+                  == offsetof(ProgHeader<float>, tier_a_present), "program header layout");
+    uint32_t v = 0, present = 0;
+    int32_t dims = 0;
+    const unsigned char* b = static_cast<const unsigned char*>(prog);
+    memcpy(&v, b + offsetof(ProgHeader<double>, merged), sizeof v);
+    memcpy(&present, b + offsetof(ProgHeader<double>, tier_a_present), sizeof present);
+    memcpy(&dims, b + offsetof(ProgHeader<double>, dims), sizeof dims);
+    if (!v)
+        return 0;
+    int types = 0;
+    for (int k = 0; k < 7; ++k)
+        types += (present >> k) & 1u;
+    return dims == 2 && types >= 5 ? 2 : 1;
 }
 
 // Hot cells: a flame's density can sit largely in a few cells (fixed

@@ -46,9 +46,10 @@ namespace {
 
 constexpr int kChunkStreams = 128;          // BLOCK of the batch kernel
 constexpr int kRoundSlots = 2;
-// dims 1..3 x merged form (FP32 programs of the seven benchmark variations)
-// off/on x colour off/on: group g = ((dims - 1) * 2 + merged) * 2 + colour
-constexpr int kGroups = 12;
+// dims 1..3 x kernel variation set (merged_for: 0 general, 1 and 2 the
+// merged-form instantiations) x colour off/on:
+// group g = ((dims - 1) * 3 + variation set) * 2 + colour
+constexpr int kGroups = 18;
 constexpr size_t kStagingBytes = 16u << 20; // device staging of one read slot
 constexpr int kReadSlots = 4;               // concurrent buffer reads
 
@@ -433,7 +434,7 @@ bool Server::launch_round_locked()
                 continue;
             SrvJob* j = cand[i];
             const SrvBuffer& b = *j->buf;
-            const int gi = ((b.flame.dims - 1) * 2 + merged_for(b.prog.data())) * 2
+            const int gi = ((b.flame.dims - 1) * 3 + merged_for(b.prog.data())) * 2
                 + (b.flame.color_dims > 0);
             if (gi != g)
                 continue;
@@ -523,7 +524,7 @@ bool Server::launch_round_locked()
     {
         if (!groups[g].n)
             continue;
-        const int dims = g / 4 + 1, merged = (g >> 1) & 1, color = g & 1;
+        const int dims = g / 6 + 1, merged = (g / 2) % 3, color = g & 1;
         const Launchers& L = launchers(o.precision, dims);
         int bps = 0, block = 0;
         e = L.occ_batch(color, merged, &bps, &block, groups[g].smem);

@@ -384,6 +384,27 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
     }
 }
 
+// julia's random bit (FlameRNG::randBool, w & 1) in lanes whose xform has
+// julia, nothing drawn in the others
+template <typename Rng>
+__device__ __forceinline__ uint32_t julia_bit(Rng& rng, bool has, bool)
+{
+    return has ? (uint32_t)(rng.next() & 1u) : 0u;
+}
+// the render kernels' generator: with the carry area in use the word is
+// known to be in the result array, so it is taken without a branch (the
+// same word next() would return)
+template <int B, int C>
+__device__ __forceinline__ uint32_t julia_bit(DevIsaac<B, C>& rng, bool has, bool carry)
+{
+    if (!carry)
+        return has ? (uint32_t)(rng.next() & 1u) : 0u;
+    const uint32_t hj = has ? 1u : 0u;
+    rng.cnt -= hj;
+    const uint64_t w = rng.Rs((int)min(rng.cnt, (uint32_t)(C - 1)));
+    return hj & (uint32_t)w;
+}
+
 // The merged form of an FP32 xform application (ProgHeader::merged):
 // v = sum over the flame's types T of coef[T] * V_T(t), each type evaluated
 // once whatever the number of variation slots, instead of one evaluation
@@ -398,11 +419,22 @@ __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R
 // has julia (coef[7], even at weight 0), at the same point of the sequence
 // as the per-slot loop (the xform's only drawing variation, so its place
 // among the slots does not matter).
-template <int D, typename Rng>
+//
+// ALL: every one of the seven types is evaluated, without a branch per type
+// (a type absent from the flame has coef 0 in every xform): one block of
+// straight-line code the compiler schedules across types, for flames that
+// use most of them.  carry: the render kernels' refill ahead guarantees
+// julia's word is in the result array (ISAAC carry area), so the draw is a
+// conditional take instead of a branch.  Neither changes which words are
+// drawn or what is added.
+template <int D, bool ALL = false, typename Rng>
 __device__ __forceinline__ bool merged_variations(const float* coef, const float* t, float* v,
-                                                  Rng& rng, uint32_t present)
+                                                  Rng& rng, uint32_t present, bool carry = false)
 {
     using T = RealTraits<float>;
+    if (ALL)
+        present = kTaLinear | kTaSinusoidal | kTaSpherical | kTaSwirl | kTaHorseshoe
+            | kTaPolar | kTaJulia;
     const float4 c0 = *reinterpret_cast<const float4*>(coef);
     const float4 c1 = *reinterpret_cast<const float4*>(coef + 4);
     const float q = nsq<D>(t);
@@ -457,9 +489,7 @@ __device__ __forceinline__ bool merged_variations(const float* coef, const float
         }
         if (present & kTaJulia)                                  /* julia 807-819 */
         {
-            float bit = 0.0f;
-            if (c1.w != 0.0f)
-                bit = (rng.next() & 1u) ? 1.0f : 0.0f;
+            const float bit = julia_bit(rng, c1.w != 0.0f, carry) ? 1.0f : 0.0f;
             float s, c;
             T::sincos_(0.5f * ang + bit * T::pi, &s, &c);
             const float k = c1.z * rt;
