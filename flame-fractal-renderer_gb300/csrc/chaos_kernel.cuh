@@ -255,6 +255,30 @@ __device__ __forceinline__ int pick_xform(const Prog<R>& pg, int nxf, Rng& rng)
     return pick_branchless(pg.thresh, nxf, rng.next() >> 11);
 }
 
+// The thresholds of a flame of up to kRegThresholds + 1 xforms held in
+// registers for a whole render (unused ones 2^64 - 1, never below m), so a
+// choice costs compares only, no shared loads: the merged-form kernels,
+// whose register budget allows it.  Same choice as pick_branchless.
+constexpr int kRegThresholds = 7;
+struct RegThresh
+{
+    uint64_t t[kRegThresholds];
+    __device__ __forceinline__ void load(const uint64_t* th, int nxf)
+    {
+#pragma unroll
+        for (int i = 0; i < kRegThresholds; ++i)
+            t[i] = i < nxf - 1 ? th[i] : ~0ull;
+    }
+    __device__ __forceinline__ int pick(uint64_t m) const
+    {
+        int x = 0;
+#pragma unroll
+        for (int i = 0; i < kRegThresholds; ++i)
+            x += m > t[i] ? 1 : 0;
+        return x;
+    }
+};
+
 template <int D, typename R>
 __device__ __forceinline__ bool bad_point(const R* p)
 {
@@ -412,6 +436,18 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
             rng.refill();
     };
 
+    // the xform choice: thresholds in registers for the all-seven merged kernels
+    // of up to kRegThresholds + 1 xforms, else shared-memory loads
+    RegThresh rth;
+    const bool reg_pick = VS == 2 && nxf <= kRegThresholds + 1;
+    if (reg_pick)
+        rth.load(pg.thresh, nxf);
+    auto choose = [&]() __attribute__((always_inline)) {
+        if (VS == 2 && reg_pick)
+            return rth.pick(rng.next() >> 11);
+        return pick_xform<R>(pg, nxf, rng);
+    };
+
     // hot-cell table: keys from a.hot_keys, counts zeroed
     unsigned int* hot = nullptr;
     if (a.hot_keys)
@@ -475,7 +511,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 for (unsigned long long k = 0; k < a.settle; ++k)
                 {
                     refill_ahead();
-                    const int xi = pick_xform<R>(pg, nxf, rng);
+                    const int xi = choose();
                     R q[D];
                     apply_xform<D, R, VS>(pg, pg.xf[xi], p, q, rng, xi, carry);
 #pragma unroll
@@ -491,7 +527,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
             for (; len > 0; --len)
             {
                 refill_ahead();
-                const int xi = pick_xform<R>(pg, nxf, rng);
+                const int xi = choose();
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
@@ -625,7 +661,9 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                             bi += di * a.mult_i[i];
                         }
                     }
-                    if (bi < a.cells)
+                    // FP32 clamps each axis index to the axis, so the cell
+                    // is always inside the buffer
+                    if (sizeof(R) == sizeof(float) || bi < a.cells)
                     {
                         bin_count(a, bi, hot);
                         if (COLOR)
@@ -722,15 +760,18 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
 // so that flames whose xforms draw equal numbers of words (16-word ISAAC
 // result arrays, about 37 KB of shared memory per CTA) run 6 CTAs per SM;
 // the FP32 body fits in 80 registers without spilling.  FP64: 4 (its body
-// needs about 120 registers; at 80 it spills).
+// needs about 120 registers; at 80 it spills).  Variation set 2 (2-D
+// merged flames of five or more types, which in practice include julia and
+// so keep the 8-word ISAAC carry: 5 CTAs per SM by shared memory): 5, which
+// leaves room for the thresholds in registers (RegThresh).
 template <typename R>
-__host__ __device__ constexpr int render_min_blocks()
+__host__ __device__ constexpr int render_min_blocks(int vs = 0)
 {
-    return sizeof(R) == 4 ? 6 : 4;
+    return sizeof(R) == 4 ? (vs == 2 ? 5 : 6) : 4;
 }
 
 template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
-__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(const RenderArgs a)
+__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>(VS)) chaos_kernel(const RenderArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     load_program<BLOCK>(smem, a.prog, a.prog_bytes);
@@ -748,7 +789,7 @@ __global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_kernel(co
 // job's arguments are copied to shared memory and its program is reloaded
 // only when the CTA moves to another job.
 template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
-__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>()) chaos_batch_kernel(const BatchArgs b)
+__global__ void __launch_bounds__(BLOCK, render_min_blocks<R>(VS)) chaos_batch_kernel(const BatchArgs b)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(16) RenderArgs s_args;
