@@ -172,7 +172,7 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     const bool merged = sizeof(R) == sizeof(float) && (MERGED || pg.merged)
         && merged_variations<D>(reinterpret_cast<const float*>(x.coef),
                                 reinterpret_cast<const float*>(t),
-                                reinterpret_cast<float*>(v), rng, pg.present);
+                                reinterpret_cast<float*>(v), rng, pg.present, carry, x.plane);
     if (merged)
         ;
     else if (pg.present == kTaLinear)

@@ -311,9 +311,10 @@ void pack_xform(const HostXform& h, int dims, XformT<R>& x, int16_t var_begin)
 } // namespace
 
 // The FP32 merged form applies (ProgHeader::merged): every variation one of
-// the seven benchmark types, 2-D types only in 2-D flames, and julia at most
-// once per xform (julia's random word differs per instance, so two julias
-// are not one julia of the summed weight; every other type is a fixed map).
+// the seven benchmark types, julia at most once per xform (julia's random
+// word differs per instance, so two julias are not one julia of the summed
+// weight; every other type is a fixed map), and above 2 dims each 2-D type
+// at most once per xform (it acts on that instance's plane).
 static bool merged_form(const HostFlame& f)
 {
     static const int32_t kTierA[7] = {V_LINEAR, V_SINUSOIDAL, V_SPHERICAL, V_SWIRL,
@@ -327,12 +328,19 @@ static bool merged_form(const HostFlame& f)
                 a = a || v.type == kTierA[k];
             if (!a)
                 return false;
-            const bool two_d = v.type == V_SWIRL || v.type == V_HORSESHOE
-                || v.type == V_POLAR || v.type == V_JULIA;
-            if (two_d && f.dims != 2)
-                return false;
             jul += v.type == V_JULIA;
         }
+        // above 2 dims each 2-D type acts on its own plane: at most one of
+        // each per xform, so one plane per type
+        if (f.dims > 2)
+            for (int32_t t2 : {V_SWIRL, V_HORSESHOE, V_POLAR})
+            {
+                int n = 0;
+                for (const auto& v : x.vars)
+                    n += v.type == t2;
+                if (n > 1)
+                    return false;
+            }
         return jul <= 1;
     };
     for (const auto& x : f.xforms)
@@ -461,6 +469,12 @@ std::vector<uint8_t> build_program(const HostFlame& f)
             continue;
         pack_xform<R>(*x, f.dims, xp[k], vb);
         if (h.merged)
+        {
+            for (int t = 0; t < 4; ++t)
+            {
+                xp[k].plane[2 * t] = 0;
+                xp[k].plane[2 * t + 1] = 1;
+            }
             for (const auto& v : x->vars)
             {
                 for (int t = 0; t < 7; ++t)
@@ -469,7 +483,15 @@ std::vector<uint8_t> build_program(const HostFlame& f)
                 // julia draws its word whatever its weight
                 if (v.type == V_JULIA)
                     xp[k].coef[7] = R(1);
+                // swirl, horseshoe, polar, julia are kTierA[3..6]
+                for (int t = 3; t < 7; ++t)
+                    if (v.type == kTierA[t] && f.dims > 2)
+                    {
+                        xp[k].plane[2 * (t - 3)] = (uint8_t)v.axis_x;
+                        xp[k].plane[2 * (t - 3) + 1] = (uint8_t)v.axis_y;
+                    }
             }
+        }
         for (const auto& v : x->vars)
         {
             VarT<R>& d = vp[vb++];

@@ -58,6 +58,9 @@ struct alignas(16) XformT
     // the type), then 1 if the xform has julia (which draws a word even at
     // weight 0), else 0
     R coef[8];
+    // merged form, 3-D flames: the plane (axis_x, axis_y) of this xform's
+    // swirl, horseshoe, polar and julia, in that order ((0, 1) where absent)
+    uint8_t plane[8];
 };
 
 // compact merged 2-D xform: pre-affine {a00, a01, b0, a10, a11, b1}, then
@@ -101,8 +104,9 @@ struct alignas(16) ProgHeader
     // 1 when the FP32 kernels evaluate each variation type once per xform
     // application and weight it by XformT::coef (variations.cuh,
     // merged_variations): FP32 programs whose variations are all benchmark
-    // types, with 2-D types only in 2-D flames and julia at most once per
-    // xform.  FP64 programs keep the reference's per-variation order.
+    // types, with julia at most once per xform and, above 2 dims, each 2-D
+    // type at most once per xform (XformT::plane).  FP64 programs keep the
+    // reference's per-variation order.
     uint32_t merged;
     // byte offset of the compact table of a merged 2-D program (kFast2Floats
     // floats per xform, the final xform last), or 0: the two affines and the

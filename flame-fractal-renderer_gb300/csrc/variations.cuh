@@ -427,9 +427,15 @@ __device__ __forceinline__ uint32_t julia_bit(DevIsaac<B, C>& rng, bool has, boo
 // julia's word is in the result array (ISAAC carry area), so the draw is a
 // conditional take instead of a branch.  Neither changes which words are
 // drawn or what is added.
+//
+// Above 2 dims each of swirl, horseshoe, polar and julia acts on its own
+// plane (XformT::plane, per lane): its coordinates are read from that plane
+// and its result added back to it (VariationFrom2D::calc_h,
+// variations.hpp:98-105), its primitives computed on that plane.
 template <int D, bool ALL = false, typename Rng>
 __device__ __forceinline__ bool merged_variations(const float* coef, const float* t, float* v,
-                                                  Rng& rng, uint32_t present, bool carry = false)
+                                                  Rng& rng, uint32_t present, bool carry = false,
+                                                  const uint8_t* planes = nullptr)
 {
     using T = RealTraits<float>;
     if (ALL)
@@ -498,6 +504,59 @@ __device__ __forceinline__ bool merged_variations(const float* coef, const float
         }
         v[0] = X;
         v[D - 1] = Y;
+    }
+    if (D > 2 && (present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+    {
+        const uint2 pl = *reinterpret_cast<const uint2*>(planes);
+        // plane k of (swirl, horseshoe, polar, julia): its x, y and a way to
+        // add (X, Y) back onto those coordinates
+        auto on_plane = [&](int k, float& x, float& y, int& ax, int& ay) {
+            const uint32_t w = k < 2 ? pl.x : pl.y;
+            ax = (int)((w >> (16 * (k & 1))) & 0xffu);
+            ay = (int)((w >> (16 * (k & 1) + 8)) & 0xffu);
+            x = coord<D>(t, ax);
+            y = coord<D>(t, ay);
+        };
+        auto add = [&](int ax, int ay, float X, float Y) {
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] += i == ax ? X : (i == ay ? Y : 0.0f);
+        };
+        float x, y;
+        int ax, ay;
+        if (present & kTaSwirl)                                  /* swirl 509-522 */
+        {
+            on_plane(0, x, y, ax, ay);
+            float s, c;
+            T::sincos_(x * x + y * y, &s, &c);
+            add(ax, ay, c0.w * (x * s - y * c), c0.w * (x * c + y * s));
+        }
+        if (present & kTaHorseshoe)                              /* horseshoe 527-540 */
+        {
+            on_plane(1, x, y, ax, ay);
+            const float q2 = x * x + y * y;
+            const float rt = q2 > 0.0f ? q2 * rsqrtf(q2) : 0.0f;
+            const float k = c1.x * T::recip_(rt + T::eps);
+            add(ax, ay, k * ((x - y) * (x + y)), k * (2.0f * x * y));
+        }
+        if (present & kTaPolar)                                  /* polar 545-555 */
+        {
+            on_plane(2, x, y, ax, ay);
+            const float q2 = x * x + y * y;
+            const float rt = q2 > 0.0f ? q2 * rsqrtf(q2) : 0.0f;
+            add(ax, ay, c1.y * (T::atan2_(y, x) * T::inv_pi), c1.y * (rt - 1.0f));
+        }
+        if (present & kTaJulia)                                  /* julia 807-819 */
+        {
+            on_plane(3, x, y, ax, ay);
+            const float bit = julia_bit(rng, c1.w != 0.0f, carry) ? 1.0f : 0.0f;
+            const float q2 = x * x + y * y;
+            const float rt = q2 > 0.0f ? q2 * rsqrtf(q2) : 0.0f;
+            float s, c;
+            T::sincos_(0.5f * T::atan2_(y, x) + bit * T::pi, &s, &c);
+            const float k = c1.z * rt;
+            add(ax, ay, k * c, k * s);
+        }
     }
     return true;
 }

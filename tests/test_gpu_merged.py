@@ -12,7 +12,8 @@ These cases aim at the edges of that claim:
   * points beyond the merged form's range (sum t_i^2 >= 1e36) fall back to
     per-slot evaluation in both instantiations alike;
   * flames using 2, 4 and 7 of the seven types (set 1 and set 2), with and
-    without a final xform, in one batch and alone.
+    without a final xform, in one batch and alone;
+  * a 3-D flame whose 2-D types act on per-variation planes.
 """
 import json
 
@@ -74,6 +75,21 @@ def render(ffr, text, kernel, n=3_000_000, seed=5):
                             traj_len=n // 4096 + 1, kernel=kernel) as r:
         s = r.render(n, seed, bad_limit=10**12)
         return s, r.counts()
+
+
+def random_3d_text():
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location(
+        "ffr_flames_t", os.path.join(here, "..", "flame-fractal-renderer_gb300", "flames.py"))
+    fl = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fl)
+    # 2-D types on random planes of a 3-D flame (the serving stream's 3-D jobs)
+    return json.dumps(fl.random_3d(5, k=5, size=(64, 64, 64)))
+
+
+CASES["random_3d_planes"] = random_3d_text()
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
