@@ -173,9 +173,7 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
         && merged_variations<D>(reinterpret_cast<const float*>(x.coef),
                                 reinterpret_cast<const float*>(t),
                                 reinterpret_cast<float*>(v), rng, pg.present, carry, x.plane);
-    if (merged)
-        ;
-    else if (pg.present == kTaLinear)
+    if (!merged && pg.present == kTaLinear)
     {
         // every variation of the flame is linear (IFS fractals): v = sum of
         // w_j * t in the reference's accumulation order, no dispatch
@@ -187,7 +185,7 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
                 v[i] += t[i] * w;
         }
     }
-    else
+    else if (!merged)
     {
         // 2-D flames: the plane primitives of the benchmark variations, once
         // per application (the same values every variation would compute)

@@ -90,6 +90,8 @@ def random_3d_text():
 
 
 CASES["random_3d_planes"] = random_3d_text()
+# more xforms than the registers hold thresholds for (shared-memory choice)
+CASES["ten_xforms"] = flame([[(TYPES[(k + j) % 7], 0.5) for j in (0, 3)] for k in range(10)])
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -147,3 +149,23 @@ def test_merged_batch_equals_solo(ffr):
                                 streams=-(-k // 4096), kernel=ffr.KERNEL_PLAIN) as r:
             r.render(k, sd, bad_limit=10**12)
             np.testing.assert_array_equal(g, r.counts())
+
+
+def test_merged_colour_flame_plain_equals_sorted(ffr):
+    """A colour flame in the merged form: counts identical, colour sums equal
+    to rounding (their atomic additions come in another order)."""
+    f = json.loads(CASES["all_seven_final"])
+    f["color_dimensions"] = 3
+    f["color_speed"] = 0.4
+    for k, x in enumerate(f["xforms"]):
+        x["color"] = [((k * 37) % 11) / 10.0, ((k * 53) % 7) / 6.0, 0.25]
+    text = json.dumps(f)
+    out = []
+    for kernel in (ffr.KERNEL_PLAIN, ffr.KERNEL_SORTED):
+        with ffr.BufferRenderer(text, precision=ffr.FP32, settle=20, streams=4096,
+                                traj_len=500, kernel=kernel) as r:
+            r.render(2_000_000, 8, bad_limit=10**12)
+            out.append(r.buffer_array())
+    np.testing.assert_array_equal(out[0][:, 0], out[1][:, 0])
+    np.testing.assert_allclose(out[0][:, 1:].copy().view(np.float64),
+                               out[1][:, 1:].copy().view(np.float64), rtol=1e-9, atol=1e-6)
