@@ -32,6 +32,10 @@ serving  the Poisson request stream twice: at 200 req/s (over capacity;
         its served rate is the capacity) and at 0.7x that capacity, each
         with p50/p99 latency and its own clock record; latency_ms at the
         top level is the sustainable stream's
+per_flame_kernels  the kernels compiled per flame at run time (NVRTC)
+        against the general plain kernel, same streams, identical buffers:
+        a random 2-D flame of twelve other variations in FP32 and the
+        benchmark flame in the FP64 mirror (3 steps each, with compile time)
 
 tv      FP32 against FP64 at a fixed sample count: total-variation distance
         between the FP32 histogram and an FP64 (reference arithmetic) one,
@@ -331,14 +335,14 @@ def run_sierpinski(args):
     sampler = ClockSampler(dev)
     sampler.start()
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
     for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
         with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
                                 device=dev, kernel=kern[args.kernel]) as r:
             ms, binned, iters, s, n_launch = _timed_steps(r, args, N, 1, flush)
             launches += n_launch
             res[name] = {"value": binned / (ms * 1e-3), "ms_per_step": ms / args.steps,
-                         "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel)}
+                         "kernel": {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel)}
             if name == "fp64" and args.verify:
                 r.clear()
                 r.render(N, 1, bad_limit=10**12)
@@ -375,7 +379,7 @@ def run_tetra3d(args):
     text = json.dumps(_flames().tetrahedron_3d((512, 512, 512)))
     B, settle = int(args.samples_per_step), 20
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
     with ffr.BufferRenderer(text, precision=ffr.FP32, settle=settle, device=dev,
                             kernel=kern[args.kernel]) as r:
         sampler = ClockSampler(dev)
@@ -398,7 +402,7 @@ def run_tetra3d(args):
     _line(args, "Sierpinski tetrahedron, 512^3 u32 buffer, 1e10 samples", value,
           ms / args.steps, "f32",
           {"samples_per_step": B, "settle": settle, "seed": 3, "streams": s.streams,
-           "traj_len": s.traj_len, "kernel": {1: "plain", 2: "xform-sorted"}.get(s.kernel),
+           "traj_len": s.traj_len, "kernel": {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel),
            "flush": "none: the 512 MiB buffer is larger than L2"},
           gpu_launches=launches,
           roofline={"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -462,6 +466,57 @@ def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8, scale=1.0):
             "tv": {"per_flame": tvs,
                    "max_ratio": max((t["ratio"] for t in tvs if t["ratio"]), default=None)},
             "clocks": clocks}
+
+
+def per_flame_record(ffr, dev, flames, steps=3):
+    """The per-flame kernels (KERNEL_JIT, NVRTC) against the general plain
+    kernel on flames the precompiled merged instantiations do not cover: a
+    random 2-D flame of parameterless variations outside the benchmark
+    seven (FP32), and the benchmark flame in the FP64 mirror.  Both kernels
+    run the same streams (the plain kernel's default plan), so their
+    buffers must be identical."""
+    import numpy as np
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    out = []
+    for name, fl, prec, n in (
+            ("random 2-D flame of 12 other variations, 1920x1080, FP32",
+             flames.random_2d(7, variations=flames.OTHER_2D), ffr.FP32, 10**9),
+            ("benchmark flame (6-xform random 1920x1080), FP64 mirror",
+             flames.random_2d(7), ffr.FP64, 10**8)):
+        text = json.dumps(fl)
+        t0 = time.perf_counter()
+        st, msg = ffr.jit_prepare(text, prec)
+        prep_s = time.perf_counter() - t0
+        if st != ffr.FFR_OK:
+            out.append({"flame": name, "error": msg})
+            continue
+        rec = {"flame": name, "samples_per_step": n, "compile_s": prep_s}
+        plan = None
+        counts = {}
+        for kname, kern in (("general", ffr.KERNEL_PLAIN), ("per_flame", ffr.KERNEL_JIT)):
+            kw = {} if plan is None else {"streams": plan[0], "traj_len": plan[1]}
+            with ffr.BufferRenderer(text, precision=prec, settle=20, device=dev, kernel=kern,
+                                    **kw) as r:
+                s = r.render(n, 99)
+                if plan is None:
+                    plan = (s.streams, s.traj_len)
+                r.clear()
+                ms, binned = 0.0, 0
+                for k in range(steps):
+                    flush.zero_()
+                    torch.cuda.synchronize()
+                    s = r.render(n, 100 + k)
+                    ms += s.kernel_ms
+                    binned += s.samples_plotted - s.dropped
+                rec[kname] = {"value": binned / (ms * 1e-3), "unit": "binned samples/s",
+                              "ms_per_step": ms / steps, "kernel": s.kernel}
+                counts[kname] = r.counts()
+        rec["speedup"] = rec["general"]["ms_per_step"] / rec["per_flame"]["ms_per_step"]
+        rec["identical_buffers"] = bool(np.array_equal(counts["general"], counts["per_flame"]))
+        rec["streams"], rec["traj_len"] = plan
+        out.append(rec)
+    return out
 
 
 def run_batch256(args):
@@ -677,7 +732,7 @@ def main():
     ap.add_argument("--serving-seconds", type=float, default=10.0,
                     help="default workload: arrival window of the over-capacity stream "
                          "(the sustainable one runs 1.5x as long)")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted", "hot"],
+    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted", "hot", "jit"],
                     help="render kernel (auto: the library's autotuner decides)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -712,7 +767,7 @@ def main():
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
     r = ffr.BufferRenderer(text, precision=prec, settle=settle, device=local,
                            kernel=kern[args.kernel])
     for w in range(args.warmup):
@@ -734,7 +789,7 @@ def main():
         iters += s.samples_iterated
         launches += 1 + s.aux_launches
         streams, traj_len = s.streams, s.traj_len
-        kernel_used = {1: "plain", 2: "xform-sorted"}.get(s.kernel) + (
+        kernel_used = {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel) + (
             " + warp-merged bins" if s.agg else "") + (
             f" + {s.hot_cells} hot cells in shared memory" if s.hot_cells else "")
     barrier()
@@ -835,8 +890,9 @@ def main():
 
     # the batched and serving paths (the 256-flame batch; the Poisson stream
     # over capacity, then at 0.7x the capacity it measured), single GPU only
-    batch = serving = None
+    batch = serving = per_flame = None
     if ws == 1 and not args.no_sub:
+        per_flame = per_flame_record(ffr, local, flames)
         batch = batch256_record(ffr, local, steps=2, warmup=1, with_tv=not args.no_tv)
         over = serving_record(ffr, local, 200.0, args.serving_seconds, 1, args.max_active,
                               with_tv=False)
@@ -880,6 +936,7 @@ def main():
         "wall_s": wall_all,
         "batch256": batch,
         "serving": serving,
+        "per_flame_kernels": per_flame,
     }
     if serving:
         line["latency_ms"] = {"p50": serving["sustainable"]["latency_ms"]["p50"],

@@ -59,11 +59,45 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
 
 
+# headers the per-flame kernels (csrc/jit.cpp, NVRTC) include, embedded in
+# the library so that it needs no source tree at run time
+JIT_HEADERS = ["std_types.h", "variation_ids.h", "flame_program.h", "isaac64.cuh", "launch.h",
+               "variations.cuh", "chaos_kernel.cuh"]
+JIT_INC = os.path.join(OUT, "jit_headers.inc")
+
+
+def _write_jit_headers() -> None:
+    """_build/jit_headers.inc: the kernel headers as raw string literals."""
+    names, texts = [], []
+    for h in JIT_HEADERS:
+        with open(os.path.join(CSRC, h)) as f:
+            t = f.read()
+        if ")FFRJIT\"" in t:
+            raise RuntimeError(f"{h} contains the raw-string delimiter")
+        names.append(f'"{h}"')
+        # split into pieces below the 64 KB literal limit some compilers keep
+        pieces = [t[i:i + 30000] for i in range(0, len(t), 30000)] or [""]
+        texts.append("\n".join(f'R"FFRJIT({p})FFRJIT"' for p in pieces))
+    out = ["// generated by build.py from csrc/: the headers of the per-flame kernels",
+           f"constexpr int kJitHeaderCount = {len(names)};",
+           "const char* const kJitHeaderNames[] = {" + ", ".join(names) + "};",
+           "const char* const kJitHeaderTexts[] = {"]
+    out += [t + "," for t in texts]
+    out.append("};")
+    text = "\n".join(out) + "\n"
+    if not os.path.exists(JIT_INC) or open(JIT_INC).read() != text:
+        tmp = JIT_INC + f".tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            f.write(text)
+        os.replace(tmp, JIT_INC)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OUT, exist_ok=True)
     hdrs = _headers()
+    _write_jit_headers()
     nv_common = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
                  "-I", CSRC, "-I", INCLUDE]
     cxx_common = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off",
@@ -85,10 +119,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src = os.path.join(CSRC, name + ".cu")
         obj = os.path.join(OUT, name + ".o")
         jobs.append((obj, [src] + hdrs, [nvcc, *nv_common, "-c", src, "-o", obj]))
-    for name in ("api", "server", "png", "flame", "json", "variations_host", "hot_cells"):
+    for name in ("api", "server", "png", "flame", "json", "variations_host", "hot_cells", "jit"):
         src = os.path.join(CSRC, name + ".cpp")
         obj = os.path.join(OUT, name + ".o")
-        jobs.append((obj, [src] + hdrs, [*cxx_common, "-c", src, "-o", obj]))
+        jobs.append((obj, [src] + hdrs + [JIT_INC], [*cxx_common, "-I", OUT, "-c", src, "-o", obj]))
     todo = [j for j in jobs if force or _stale(j[0], j[1])]
     if todo:
         workers = min(len(todo), max(2, os.cpu_count() or 2))

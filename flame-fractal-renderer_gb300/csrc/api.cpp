@@ -20,6 +20,7 @@
 
 #include "flame.hpp"
 #include "isaac64.cuh"
+#include "jit.h"
 #include "launch.h"
 
 namespace ffr {
@@ -145,6 +146,11 @@ struct ffr_ctx
     unsigned int* d_hot = nullptr;
     unsigned int hot_mult = 0;
     int hot_cells = 0;
+    // the per-flame kernel (jit.h), once compiled and loaded for this
+    // context's flame structure; jit_source is empty for programs that have
+    // none (the FP32 merged form)
+    const JitKernel* jit = nullptr;
+    std::string jit_source;
     // kernels launched by the current call besides the render kernel
     unsigned int aux_launches = 0;
     std::string err = "no error";
@@ -326,6 +332,21 @@ int program_words(const ffr_ctx* c)
     return (int)h->rng_words_max;       // same offset in the float header
 }
 
+// The per-flame kernel of the context's program, compiled on first use (or
+// found in the caches); ready_only: only if no compile is needed
+ffr_status ensure_jit(ffr_ctx* c, bool ready_only = false)
+{
+    if (c->jit)
+        return FFR_OK;
+    if (c->jit_source.empty())
+        c->jit_source = jit_source(c->prog_host, c->opts.precision, c->flame.color_dims > 0);
+    std::string err;
+    c->jit = jit_kernel(c->jit_source, c->opts.precision, &err, !ready_only);
+    if (!c->jit)
+        return ready_only ? FFR_ERR_ARG : fail(c, FFR_ERR_CUDA, err);
+    return FFR_OK;
+}
+
 // Launch plan: kernel, streams, trajectory length and grid.  The hot-cell
 // table's shared memory is planned for FFR_KERNEL_HOT and when *hot is set
 // on entry, for the plain kernel with fewer than 2^30 cells and fewer than
@@ -346,7 +367,20 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     const unsigned int pb = prog_smem_for(c->prog_host.data());
     const int nxf = (int)c->flame.xforms.size();
     int k = kreq;
-    if (k != FFR_KERNEL_PLAIN && !c->L().occ_sorted)
+    if (k == FFR_KERNEL_JIT)
+    {
+        // programs in the FP32 merged form have no per-flame kernel: their
+        // precompiled instantiation already runs without type dispatch
+        if (merged_for(c->prog_host.data()))
+            k = FFR_KERNEL_PLAIN;
+        else
+        {
+            ffr_status js = ensure_jit(c);
+            if (js != FFR_OK)
+                return js;
+        }
+    }
+    if (k != FFR_KERNEL_PLAIN && k != FFR_KERNEL_JIT && !c->L().occ_sorted)
     {
         // no xform-sorted instantiation for this dimension count
         if (k == FFR_KERNEL_SORTED)
@@ -354,7 +388,7 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
                 "(dims " + std::to_string(c->flame.dims) + ": plain kernel only)");
         k = FFR_KERNEL_PLAIN;
     }
-    if (k != FFR_KERNEL_PLAIN)
+    if (k != FFR_KERNEL_PLAIN && k != FFR_KERNEL_JIT)
     {
         CU(c, c->L().occ_sorted(color, spill, &bps, &block, pb, nxf, program_words(c), &smem));
         if (bps >= 1)
@@ -365,11 +399,17 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
         else
             k = FFR_KERNEL_PLAIN;
     }
-    const bool use_hot = want_hot && k == FFR_KERNEL_PLAIN;
+    const bool use_hot = want_hot && (k == FFR_KERNEL_PLAIN || k == FFR_KERNEL_JIT);
     if (k == FFR_KERNEL_PLAIN)
         CU(c, c->L().occ(color, merged_for(c->prog_host.data()),
                          rsl_words_for(c->prog_host.data()), use_hot ? 1 : 0, &bps,
                          &block, pb, nxf, &smem));
+    else if (k == FFR_KERNEL_JIT)
+    {
+        block = kJitBlock;
+        smem = chaos_smem_bytes<kJitBlock>(pb, nxf, rsl_words_for(c->prog_host.data()), use_hot);
+        CU(c, jit_occupancy(c->jit, smem, &bps));
+    }
     *kernel = k;
     if (bps < 1)
         return fail(c, FFR_ERR_ARG, "render kernel does not fit on an SM "
@@ -460,6 +500,19 @@ void fill_args(ffr_ctx* c, RenderArgs& a, uint64_t samples, uint64_t seed, uint6
     a.merged = merged_for(c->prog_host.data());
     std::memcpy(a.isaac_init, c->isaac_init, sizeof a.isaac_init);
     set_geometry(a, c->prog_host.data(), c->opts.precision);
+}
+
+// one render launch of the planned kernel on the context stream
+cudaError_t launch_render_kernel(ffr_ctx* c, int kernel, const RenderArgs& a, int grid)
+{
+    if (kernel == FFR_KERNEL_SORTED)
+        return c->L().sorted(a, grid, c->stream);
+    if (kernel == FFR_KERNEL_JIT)
+        return jit_launch(c->jit, a, grid,
+                          chaos_smem_bytes<kJitBlock>(a.prog_bytes, a.nxf, a.rsl_words,
+                                                      a.hot_keys != nullptr),
+                          c->stream);
+    return c->L().render(a, grid, c->stream);
 }
 
 // the leading fields of DevStats (everything before xf_dist)
@@ -763,8 +816,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
             if (st != FFR_OK)
                 return st;
             CU(c, cudaEventRecord(c->ev0, c->stream));
-            CU(c, kk == FFR_KERNEL_SORTED ? c->L().sorted(a, grid, c->stream)
-                                          : c->L().render(a, grid, c->stream));
+            CU(c, launch_render_kernel(c, kk, a, grid));
             ++c->aux_launches;
             CU(c, cudaEventRecord(c->ev1, c->stream));
             CU(c, cudaEventSynchronize(c->ev1));
@@ -779,9 +831,13 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         }
         return FFR_OK;
     };
-    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED})
+    // the per-flame kernel is a candidate when it is compiled already (an
+    // earlier FFR_KERNEL_JIT render or ffr_jit_prepare, in this process or
+    // in the FFR_JIT_CACHE directory): the autotuner never waits for NVRTC
+    const bool jit_ready = !merged_for(c->prog_host.data()) && ensure_jit(c, true) == FFR_OK;
+    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED, FFR_KERNEL_JIT})
         for (int g : {0, 1})
-            if (st == FFR_OK)
+            if (st == FFR_OK && (k != FFR_KERNEL_JIT || jit_ready))
                 st = probe(k, g, false);
     // the probes' counts (u32: far below 2^32 per cell) locate hot cells
     unsigned int mult = 0;
@@ -791,9 +847,10 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     if (st == FFR_OK)
         st = set_hot(c, mult, keys);
     if (st == FFR_OK && mult)
-        for (int g : {0, 1})
-            if (st == FFR_OK)
-                st = probe(FFR_KERNEL_PLAIN, g, true);
+        for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_JIT})
+            for (int g : {0, 1})
+                if (st == FFR_OK && (k != FFR_KERNEL_JIT || jit_ready))
+                    st = probe(k, g, true);
     // launch shape for the best candidate: fewer resident CTAs per SM, each
     // thread then running more streams one after another (the streams, and
     // so the buffer, stay the same); kept only when 3% faster
@@ -887,7 +944,7 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: ABI version mismatch");
     if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown precision");
-    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_HOT)
+    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_JIT)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown kernel");
     ffr_ctx* c = new (std::nothrow) ffr_ctx;
     if (!c)
@@ -972,6 +1029,39 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
 void ffr_destroy(ffr_ctx* c)
 {
     destroy(c);
+}
+
+ffr_status ffr_jit_prepare(const char* json, size_t len, const ffr_opts* opts)
+{
+    if (!json)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_jit_prepare: json is NULL");
+    ffr_opts o;
+    if (opts)
+        o = *opts;
+    else
+        ffr_default_opts(&o);
+    if (o.abi_version != FFR_ABI_VERSION)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_jit_prepare: ABI version mismatch");
+    if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
+        return fail(nullptr, FFR_ERR_ARG, "ffr_jit_prepare: unknown precision");
+    std::string src;
+    try
+    {
+        const HostFlame f = parse_flame(std::string(json, len));
+        const std::vector<uint8_t> prog = o.precision == FFR_FP64 ? build_program<double>(f)
+                                                                  : build_program<float>(f);
+        src = jit_source(prog, o.precision, f.color_dims > 0);
+    }
+    catch (const std::exception& e)
+    {
+        return fail(nullptr, FFR_ERR_PARSE, e.what());
+    }
+    if (src.empty())
+        return FFR_OK;      // FP32 merged form: no per-flame kernel
+    std::string err;
+    if (!jit_compile_only(src, o.precision, &err))
+        return fail(nullptr, FFR_ERR_CUDA, err);
+    return FFR_OK;
 }
 
 const char* ffr_last_error(const ffr_ctx* c)
@@ -1157,10 +1247,7 @@ ffr_status ffr_render(ffr_ctx* c, uint64_t samples, uint64_t seed, uint64_t bad_
     }
     *c->h_cancel = 0u;
     CU(c, cudaEventRecord(c->ev0, c->stream));
-    if (kernel == FFR_KERNEL_SORTED)
-        CU(c, c->L().sorted(a, grid, c->stream));
-    else
-        CU(c, c->L().render(a, grid, c->stream));
+    CU(c, launch_render_kernel(c, kernel, a, grid));
     CU(c, cudaEventRecord(c->ev1, c->stream));
     s = wait_stream(c);
     c->count_bound += samples;

@@ -17,7 +17,7 @@
 // returned old value carries into the u32 high-word buffer).
 #pragma once
 
-#include <cstdint>
+#include "std_types.h"
 
 #include "flame_program.h"
 #include "isaac64.cuh"
@@ -227,6 +227,146 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     }
 }
 
+// Per-flame kernels (compiled at run time for one flame, jit.cpp).  A spec
+// type SP fixes at compile time, for each variation slot k (the k-th
+// variation of an xform), the types that slot holds in the flame's xforms,
+// and the flame's kTa* bits (SP::present) and largest variation count
+// (SP::slots).  apply_xform_spec is apply_xform's general path with the
+// 98-way type switch of each slot narrowed to those types and the
+// benchmark types' shared body to the ones the slot holds.  Everything
+// else -- affines, plane primitives, the slot loop -- stays common to all
+// lanes of a warp, as in apply_xform (code specialised per xform instead
+// would run each xform's affines and primitives one xform after another
+// in a warp whose lanes chose different xforms).  The arithmetic is
+// apply_xform's on the same program data, so the buffers are the general
+// kernel's.
+struct NoSpec
+{
+    static constexpr bool on = false;
+};
+
+// o = V(t) for a variation of one of the types TYPES... or, when TA is not
+// 0, of a benchmark type in TA (kTa* bits)
+template <int D, typename R, uint32_t TA, int... TYPES>
+struct SlotTypes
+{
+    template <typename Rng>
+    __device__ static __forceinline__ void eval(const VarT<R>& var, const R* t, R* o, Rng& rng,
+                                                const PlanePrims<R>& pp)
+    {
+        variation_tier_a<D, R>(var, t, o, rng, TA, pp);
+    }
+};
+
+template <int D, typename R, uint32_t TA, int T0, int... REST>
+struct SlotTypes<D, R, TA, T0, REST...>
+{
+    template <typename Rng>
+    __device__ static __forceinline__ void eval(const VarT<R>& var, const R* t, R* o, Rng& rng,
+                                                const PlanePrims<R>& pp)
+    {
+        if constexpr (TA == 0 && sizeof...(REST) == 0)
+            variation<D, R, T0>(var, t, o, rng, 0u, pp);    // the slot's only type
+        else
+        {
+            if (var.type == T0)
+                variation<D, R, T0>(var, t, o, rng, TA, pp);
+            else
+                SlotTypes<D, R, TA, REST...>::eval(var, t, o, rng, pp);
+        }
+    }
+};
+
+// slots S..SP::slots-1 of an xform of n variations from pg.var[vb] on
+template <typename SP, int S, int D, typename R, typename Rng>
+__device__ __forceinline__ void spec_slots(const Prog<R>& pg, int vb, int n, const R* t, R* v,
+                                           Rng& rng, const PlanePrims<R>& pp)
+{
+    if constexpr (S < SP::slots)
+    {
+        if (S < n)
+        {
+            const VarT<R>& var = pg.var[vb + S];
+            R o[D];
+            SP::template slot<S, D, R>(var, t, o, rng, pp);
+            const R w = var.weight;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] += o[i] * w;
+            spec_slots<SP, S + 1, D, R>(pg, vb, n, t, v, rng, pp);
+        }
+    }
+}
+
+// XForm::applyIteration through the flame's spec (apply_xform's general path)
+template <int D, typename R, typename SP, typename Rng>
+__device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT<R>& x,
+                                                 const R* p, R* out, Rng& rng)
+{
+    R t[D], v[D];
+    if (D < 3 || x.has_pre)
+        affine<D>(x.pre, p, t);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            t[i] = p[i];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        v[i] = R(0);
+    const int vb = x.var_begin, n = x.var_count;
+    if constexpr (SP::present == kTaLinear)
+    {
+        // every variation of the flame is linear (apply_xform's IFS loop)
+        for (int k = vb; k < vb + n; ++k)
+        {
+            const R w = pg.var[k].weight;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] += t[i] * w;
+        }
+    }
+    else
+    {
+        PlanePrims<R> pp;
+        pp.valid = false;
+        pp.q = pp.rt = pp.ang = R(0);
+        if constexpr (D == 2 && (SP::present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+        {
+            using T = RealTraits<R>;
+            const R px = t[0], py = t[D - 1];
+            pp.valid = true;
+            pp.q = px * px + py * py;
+            if (SP::present & (kTaHorseshoe | kTaPolar | kTaJulia))
+                pp.rt = T::sqrt_(pp.q);
+            if (SP::present & (kTaPolar | kTaJulia))
+                pp.ang = T::atan2_(py, px);
+        }
+        spec_slots<SP, 0, D, R>(pg, vb, n, t, v, rng, pp);
+    }
+    if (D < 3 || x.has_post)
+        affine<D>(x.post, v, out);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            out[i] = v[i];
+    }
+}
+
+// one xform application in the render loop: the flame's own code (SP), or
+// apply_xform
+template <int D, typename R, int VS, typename SP, typename Rng>
+__device__ __forceinline__ void xform_step(const Prog<R>& pg, const XformT<R>& x, int xi,
+                                           const R* p, R* out, Rng& rng, bool carry)
+{
+    if constexpr (SP::on)
+        apply_xform_spec<D, R, SP>(pg, x, p, out, rng);
+    else
+        apply_xform<D, R, VS>(pg, x, p, out, rng, xi, carry);
+}
+
 // first i with m <= thresh[i]: the thresholds of the first nxf-1 xforms are
 // non-decreasing (prefix sums of non-negative weights) and the last is 2^53,
 // so the index is the number of leading thresholds below m.  A fixed-trip
@@ -376,7 +516,7 @@ __device__ __forceinline__ void bin_count(const RenderArgs& a, uint64_t bi, unsi
 
 // Runs streams s_first, s_first + s_stride, ... (below the job's active
 // stream count), then merges this CTA's statistics into a.stats.
-template <int D, typename R, bool COLOR, int BLOCK, int VS = 0>
+template <int D, typename R, bool COLOR, int BLOCK, int VS = 0, typename SP = NoSpec>
 __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* smem,
                                            unsigned long long s_first,
                                            unsigned long long s_stride)
@@ -511,7 +651,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     refill_ahead();
                     const int xi = choose();
                     R q[D];
-                    apply_xform<D, R, VS>(pg, pg.xf[xi], p, q, rng, xi, carry);
+                    xform_step<D, R, VS, SP>(pg, pg.xf[xi], xi, p, q, rng, carry);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -529,7 +669,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 const XformT<R>& xf = pg.xf[xi];
                 {
                     R q[D];
-                    apply_xform<D, R, VS>(pg, xf, p, q, rng, xi, carry);
+                    xform_step<D, R, VS, SP>(pg, xf, xi, p, q, rng, carry);
 #pragma unroll
                     for (int i = 0; i < D; ++i)
                         p[i] = q[i];
@@ -544,7 +684,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                 if (h.has_final)
                 {
                     const XformT<R>& ff = pg.xf[nxf];
-                    apply_xform<D, R, VS>(pg, ff, p, pf, rng, nxf, carry);
+                    xform_step<D, R, VS, SP>(pg, ff, nxf, p, pf, rng, carry);
                     if (COLOR)
                     {
                         if (ff.has_color)

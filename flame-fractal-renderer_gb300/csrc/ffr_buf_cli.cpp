@@ -26,7 +26,8 @@
 // (default 53 = settle_iters<double>), --streams N, --trajectories T (T
 // streams of one trajectory each, of ceil(samples / T) samples: "N samples
 // from T trajectories"; excludes -b and --streams), --device N,
-// --timeout-ms N.
+// --timeout-ms N, --kernel auto|plain|sorted|hot|jit (ffr_opts.kernel; jit =
+// the kernel compiled for this flame's structure at run time).
 //
 // Errors: the reference lets parse/IO exceptions escape main (abort); this
 // front end prints "ERROR: <message>" and exits 1.  A bad-value stop prints
@@ -66,6 +67,7 @@ struct Args
     uint64_t trajectories = 0;
     int device = 0;
     uint64_t timeout_ms = 0;
+    int kernel = FFR_KERNEL_AUTO;
     bool help = false;
     bool have_flame = false, have_output = false;
 };
@@ -86,7 +88,8 @@ const char* kUsage =
     "  --streams arg (=0)            concurrent RNG streams (0 = device)\n"
     "  --trajectories arg            trajectories (one stream each)\n"
     "  --device arg (=0)             CUDA device\n"
-    "  --timeout-ms arg (=0)         render time limit (0 = none)\n";
+    "  --timeout-ms arg (=0)         render time limit (0 = none)\n"
+    "  --kernel arg (=auto)          auto, plain, sorted, hot or jit\n";
 
 [[noreturn]] void die(const std::string& m)
 {
@@ -116,7 +119,7 @@ Args parse_args(int argc, char** argv)
         {"batch-size", 'b', true}, {"bad-values", 'z', true},
         {"seed", 0, true}, {"precision", 0, true}, {"settle", 0, true},
         {"streams", 0, true}, {"trajectories", 0, true}, {"device", 0, true},
-        {"timeout-ms", 0, true},
+        {"timeout-ms", 0, true}, {"kernel", 0, true},
     };
     for (int k = 1; k < argc; ++k)
     {
@@ -183,6 +186,18 @@ Args parse_args(int argc, char** argv)
         else if (n == "trajectories") a.trajectories = to_u64(val, n);
         else if (n == "device") a.device = (int)to_u64(val, n);
         else if (n == "timeout-ms") a.timeout_ms = to_u64(val, n);
+        else if (n == "kernel")
+        {
+            static_assert(FFR_KERNEL_AUTO == 0 && FFR_KERNEL_JIT == 4, "kernel names");
+            static const char* const kNames[] = {"auto", "plain", "sorted", "hot", "jit"};
+            int k = -1;
+            for (int i = 0; i < 5; ++i)
+                if (val == kNames[i])
+                    k = i;
+            if (k < 0)
+                die("--kernel must be auto, plain, sorted, hot or jit");
+            a.kernel = k;       // FFR_KERNEL_AUTO .. FFR_KERNEL_JIT in this order
+        }
     }
     return a;
 }
@@ -285,6 +300,7 @@ int main(int argc, char** argv)
     o.streams = a.streams;
     o.traj_len = a.batch;
     o.timeout_ms = a.timeout_ms;
+    o.kernel = a.kernel;
     ffr_ctx* ctx = nullptr;
     ffr_status st = ffr_create(text.data(), text.size(), &o, &ctx);
     if (st != FFR_OK)

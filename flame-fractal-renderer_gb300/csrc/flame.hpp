@@ -60,6 +60,9 @@ HostFlame parse_flame(const std::string& json_text);
 // (Variation::parseVariation, variations.hpp:2614-2626).
 HostVar parse_variation(const JsonValue& j, int dims);
 
+// The JSON name of a variation id ("?" outside 0..V_COUNT-1)
+const char* variation_name(int id);
+
 // Pack the flame into a program blob of arithmetic type R.
 template <typename R>
 std::vector<uint8_t> build_program(const HostFlame& f);

@@ -23,7 +23,7 @@
 // m <= thresh[i]: the same choice for every word, in integer arithmetic.
 #pragma once
 
-#include <cstdint>
+#include "std_types.h"
 
 #include "variation_ids.h"
 

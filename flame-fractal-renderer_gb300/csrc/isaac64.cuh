@@ -25,7 +25,7 @@
 // what happens once lanes draw different numbers of words per step.
 #pragma once
 
-#include <cstdint>
+#include "std_types.h"
 
 namespace ffr {
 

@@ -1,15 +1,17 @@
 // Interface between the host runtime (api.cpp) and the kernel translation
-// units.  Plain structs shared by host and device code.
+// units.  Plain structs shared by host and device code; the run-time
+// compiled kernels (NVRTC, jit.cpp) see only those and the device helpers
+// (the host-only parts are left out under __CUDACC_RTC__).
 #pragma once
 
-#include <cstddef>
-#include <cstdint>
-#include <cstring>
+#include "std_types.h"
+#ifndef __CUDACC_RTC__
 #include <functional>
 #include <queue>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
+#endif
 
 #include "flame_program.h"
 
@@ -73,6 +75,7 @@ struct RenderArgs
     unsigned long long cells;
 };
 
+#ifndef __CUDACC_RTC__
 // copy the geometry of a program blob (precision 0 FP64, 1 FP32) into a
 inline void set_geometry(RenderArgs& a, const void* prog, int precision)
 {
@@ -105,6 +108,7 @@ inline void set_geometry(RenderArgs& a, const void* prog, int precision)
         a.cells = h.cells;
     }
 }
+#endif
 
 // xform counting in the render kernels: flames of up to kPackedXfCounters
 // xforms count in eight 8-bit fields of one register per thread (flushed
@@ -118,6 +122,7 @@ constexpr int kLocalXfCounters = 16;
 // (not 16) keeps such flames at 5 CTAs of 128 threads per SM.
 constexpr int kIsaacRslMax = 24;
 
+#ifndef __CUDACC_RTC__
 // result-array words for a program blob (16 or kIsaacRslMax)
 inline int rsl_words_for(const void* prog)
 {
@@ -128,9 +133,11 @@ inline int rsl_words_for(const void* prog)
            sizeof v);
     return v ? kIsaacRslMax : 16;
 }
+#endif
 
 __host__ __device__ inline unsigned int align16u(unsigned int x) { return (x + 15u) & ~15u; }
 
+#ifndef __CUDACC_RTC__
 // ProgHeader::smem_bytes of a program blob: the part the kernels copy into
 // shared memory (RenderArgs::prog_bytes)
 inline unsigned int prog_smem_for(const void* prog)
@@ -167,6 +174,7 @@ inline int merged_for(const void* prog)
         types += (present >> k) & 1u;
     return dims == 2 && types >= 5 ? 2 : 1;
 }
+#endif
 
 // Hot cells: a flame's density can sit largely in a few cells (fixed
 // points, attractor cores; the 1920x1080 benchmark flame puts 18% of its
@@ -184,6 +192,7 @@ constexpr unsigned int kHotEmpty = 0xFFFFFFFFu;
 // candidates a hot-cell search collects at most per threshold
 constexpr unsigned int kHotCollectCap = 1024;
 
+#ifndef __CUDACC_RTC__
 // Hot-cell table from candidate cells (count << 32 | cell, any order, from
 // launch_hot_collect) of a buffer holding about sum samples: the up to
 // kHotCells hottest, if together they hold at least 1/50 of sum, placed by
@@ -192,6 +201,7 @@ constexpr unsigned int kHotCollectCap = 1024;
 // and the result is true; found is sorted hottest first.
 bool hot_place(std::vector<unsigned long long>& found, unsigned long long sum,
                unsigned int* mult, std::vector<unsigned int>& keys);
+#endif
 
 // Dynamic shared memory of the plain and batch render kernels: the program,
 // ISAAC state (randmem [16][BLOCK], results [rsl_words][BLOCK]), the
@@ -245,6 +255,7 @@ struct BatchArgs
     const unsigned long long* order;
 };
 
+#ifndef __CUDACC_RTC__
 // Claim order for jobs of chunks[k] chunks: chunk r of job k gets the key
 // (r + 1/2) / chunks[k] and claims run in ascending key order (ties by job),
 // so every job advances at the same relative pace and concurrent CTAs spread
@@ -280,6 +291,7 @@ inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
         }
     }
 }
+#endif
 
 // Single xform application on a batch of points (one stream per point).
 struct StepArgs
@@ -307,11 +319,13 @@ struct TraceArgs
     unsigned long long isaac_init[16];
 };
 
+#ifndef __CUDACC_RTC__
 // Isaac::init with flag = false: the 16-word randmem every stream starts from
 void isaac_init_table(unsigned long long out[16]);
 
 // set the message ffr_last_error(NULL) returns on this thread
 void set_global_error(const std::string& m);
+#endif
 
 // the 16-word randmem table every stream starts from (isaac64.cuh)
 struct IsaacInit
@@ -329,8 +343,11 @@ struct IsaacInit
 // (a uniform Sierpinski triangle: 1.9 ms merged, 1.1 ms unmerged per 1e8
 // samples), so both bin unmerged (agg_after_search).
 constexpr int kDefaultAgg = 1;
+#ifndef __CUDACC_RTC__
 inline int agg_after_search(bool searched) { return searched ? 0 : kDefaultAgg; }
+#endif
 
+#ifndef __CUDACC_RTC__
 // precision: 0 = FP64 mirror, 1 = FP32
 #define FFR_DECLARE_LAUNCHERS(P, D)                                              \
     cudaError_t launch_render_p##P##_d##D(const RenderArgs&, int grid,          \
@@ -437,6 +454,8 @@ cudaError_t launch_image(void* out, int bits, unsigned long long cells, int mode
 
 // zero one statistics block (nxf per-xform counters), extremes to +/-inf
 cudaError_t launch_stats_reset(DevStats* st, int nxf, cudaStream_t);
+
+#endif
 
 // monotone u64 key of a double (NaN never stored)
 __host__ __device__ inline unsigned long long order_key(double d)

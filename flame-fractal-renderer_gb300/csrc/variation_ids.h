@@ -5,7 +5,7 @@
 // three-dimensional factory is empty (variations.hpp:2559-2564).
 #pragma once
 
-#include <cstdint>
+#include "std_types.h"
 
 namespace ffr {
 

@@ -9,7 +9,7 @@
 // VariationFrom2D::calc_h does, variations.hpp:98-105).
 #pragma once
 
-#include <cstdint>
+#include "std_types.h"
 
 #include "flame_program.h"
 #include "isaac64.cuh"
@@ -266,12 +266,12 @@ struct PlanePrims
 // its reference expression in the reference's operation order (the FP64
 // results are bit-identical to the switch), and julia draws its word at the
 // same point of the RNG sequence.
-template <int D, typename R, typename Rng>
+template <int D, typename R, int FIXED = -1, typename Rng>
 __device__ __forceinline__ void variation_tier_a(const VarT<R>& v, const R* t, R* out, Rng& rng,
                                                  uint32_t present, const PlanePrims<R>& pp)
 {
     using T = RealTraits<R>;
-    const int ty = v.type;
+    const int ty = FIXED >= 0 ? FIXED : v.type;
     const bool is_sin = ty == V_SINUSOIDAL, is_sph = ty == V_SPHERICAL;
     if (!(present & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
     {
@@ -567,14 +567,19 @@ __device__ __forceinline__ bool merged_variations(const float* coef, const float
 // Point::operator/= does (src/types/point.hpp:127-131).  RNG draws go
 // through rng.next() in the reference's order (FlameRNG,
 // src/rng/flame_rng.hpp).
-template <int D, typename R, typename Rng>
+//
+// FIXED >= 0: the variation's type is FIXED, known when the kernel is
+// compiled (the per-flame kernels, jit.cpp); the same expressions as for a
+// type read from v, with the other types' code left out.
+template <int D, typename R, int FIXED = -1, typename Rng>
 __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rng& rng,
                                           uint32_t present, const PlanePrims<R>& pp)
 {
     using T = RealTraits<R>;
-    if (tier_a(v.type))
+    const int vtype = FIXED >= 0 ? FIXED : v.type;
+    if (tier_a(vtype))
     {
-        variation_tier_a<D, R>(v, t, o, rng, present, pp);
+        variation_tier_a<D, R, FIXED>(v, t, o, rng, present, pp);
         return;
     }
     const int ax = v.axis_x, ay = v.axis_y;
@@ -582,8 +587,8 @@ __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rn
 
     const R* P = v.p;
     R x, y, r, a, s, c, X = R(0), Y = R(0), d;
-        if (v.type < kFirst2D) {
-        switch (v.type) {
+        if (vtype < kFirst2D) {
+        switch (vtype) {
         case V_LINEAR: /* 169-177 */
             for (int i = 0; i < D; ++i) out[i] = t[i];
             return;
@@ -695,7 +700,7 @@ __device__ __forceinline__ void variation(const VarT<R>& v, const R* t, R* o, Rn
 #define R2SQ (x * x + y * y)
 #define R2 T::sqrt_(x * x + y * y)
 #define ANG T::atan2_(y, x)
-    switch (v.type) {
+    switch (vtype) {
     case V_SWIRL: /* 509-522 */
         r = R2SQ; T::sincos_(r, &s, &c);
         X = x * s - y * c; Y = x * c + y * s; break;

@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libffr_gpu.so")
 CLI_PATH = os.path.join(HERE, "_build", "ffr-buf")
 
-FFR_ABI_VERSION = 3
+FFR_ABI_VERSION = 4
 MAX_DIMS = 4
 MAX_XFORM_IDS = 4096
 MAX_BAD_RECORDS = 4096
@@ -31,11 +31,11 @@ STATUS_NAMES = ["FFR_OK", "FFR_BAD_VALUES", "FFR_ERR_PARSE", "FFR_ERR_ARG",
                 "FFR_ERR_IO", "FFR_ERR_OOM", "FFR_ERR_TIMEOUT", "FFR_ERR_CUDA",
                 "FFR_ERR_STATE"]
 FP64, FP32 = 0, 1
-KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED, KERNEL_HOT = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED, KERNEL_HOT, KERNEL_JIT = 0, 1, 2, 3, 4
 
 # every symbol include/ffr_gpu.h declares
 EXPORTS = [
-    "ffr_default_opts", "ffr_create", "ffr_destroy", "ffr_last_error",
+    "ffr_default_opts", "ffr_create", "ffr_destroy", "ffr_jit_prepare", "ffr_last_error",
     "ffr_info", "ffr_size", "ffr_flame_json", "ffr_add_buffer", "ffr_render",
     "ffr_read_buffer", "ffr_load_buffer", "ffr_histogram", "ffr_clear",
     "ffr_isaac_words", "ffr_step", "ffr_trace", "ffr_plan",
@@ -129,6 +129,7 @@ def load_library(path: str = LIB_PATH):
         L.ffr_create.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts), ctypes.POINTER(vp)]
         L.ffr_destroy.argtypes = [vp]
         L.ffr_destroy.restype = None
+        L.ffr_jit_prepare.argtypes = [ctypes.c_char_p, sz, ctypes.POINTER(Opts)]
         L.ffr_last_error.argtypes = [vp]
         L.ffr_last_error.restype = ctypes.c_char_p
         L.ffr_info.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64),
@@ -411,6 +412,18 @@ def create_status(flame_text: str, precision: int = FP64):
     if st == FFR_OK:
         lib.ffr_destroy(ctx)
     return st, msg
+
+
+def jit_prepare(flame_text: str, precision: int = FP64):
+    """(status, message) of ffr_jit_prepare: compile the flame's per-flame
+    kernel (KERNEL_JIT) with NVRTC, without a device."""
+    lib = load_library()
+    raw = flame_text.encode("utf-8")
+    o = Opts()
+    lib.ffr_default_opts(ctypes.byref(o))
+    o.precision = precision
+    st = lib.ffr_jit_prepare(raw, len(raw), ctypes.byref(o))
+    return st, lib.ffr_last_error(None).decode("utf-8", "replace")
 
 
 class Batch:

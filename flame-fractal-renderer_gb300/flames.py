@@ -15,6 +15,9 @@ every machine.
                      weights Dirichlet(1); bounds [-2,2] x [-1.125,1.125]
   random_3d          the 3-D analogue (2-D variations act on a random plane,
                      given by axis_x / axis_y)
+  random_2d(..., variations=OTHER_2D)
+                     the same with twelve parameterless variations outside
+                     the benchmark seven (the per-flame kernel workload)
   batch_jobs         the 256-flame batch: random_2d flames with 2..8 xforms,
                      square buffers of side log-uniform in [256, 2048],
                      sample counts log-uniform in [1e7, 1e9]
@@ -29,6 +32,10 @@ import numpy as np
 
 TIER_A = ["linear", "sinusoidal", "spherical", "swirl", "horseshoe", "polar", "julia"]
 TWO_D = {"swirl", "horseshoe", "polar", "julia"}
+# twelve 2-D variations outside the benchmark seven that take no parameters
+# (the per-flame kernel workload: random_2d(seed, variations=OTHER_2D))
+OTHER_2D = ["handkerchief", "heart", "disc", "spiral", "hyperbolic", "diamond", "ex",
+            "exponential", "cosine", "power", "cylinder", "tangent"]
 
 
 def _f(x) -> float:

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FFR_ABI_VERSION 3
+#define FFR_ABI_VERSION 4
 
 typedef enum ffr_status {
     FFR_OK = 0,
@@ -91,9 +91,19 @@ typedef struct ffr_opts {
    cell table or not), else plain (FP32) or sorted where it fits (FP64).
    HOT: the plain kernel counting the flame's hottest cells (found by one
    probe render) in per-CTA shared memory, without warp merging; streams
-   are planned with that memory reserved.  All choices give identical buffers for equal streams
-   and trajectory lengths. */
-enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2, FFR_KERNEL_HOT = 3 };
+   are planned with that memory reserved.  JIT: the plain kernel compiled
+   for this flame's structure at run time (NVRTC; each xform's variation
+   types fixed in the code instead of dispatched per variation, as the
+   reference's XForm::applyIteration, src/types/xform.hpp:211-227,
+   dispatches through virtual calls), compiled on the first render that
+   needs it unless ffr_jit_prepare compiled it, cached per process and, with
+   FFR_JIT_CACHE naming a directory, on disk; FP32 programs of the seven
+   benchmark variations run their precompiled merged instantiation instead
+   (stats.kernel PLAIN).  AUTO also times the JIT kernel when it is already
+   compiled.  All choices give identical buffers for equal streams and
+   trajectory lengths. */
+enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2, FFR_KERNEL_HOT = 3,
+       FFR_KERNEL_JIT = 4 };
 
 typedef struct ffr_stats {
     uint64_t samples_iterated;   /* getSamplesIterated */
@@ -113,7 +123,7 @@ typedef struct ffr_stats {
     uint64_t traj_len;
     uint64_t settle;
     double kernel_ms;            /* device time of the render kernel(s) */
-    int32_t kernel;              /* FFR_KERNEL_PLAIN or FFR_KERNEL_SORTED */
+    int32_t kernel;              /* FFR_KERNEL_PLAIN, _SORTED or _JIT */
     int32_t agg;                 /* 1: equal-cell increments were warp-merged */
     int32_t hot_cells;           /* cells counted in per-CTA shared memory
                                     (the autotuner's hot-cell table), or 0 */
@@ -143,6 +153,17 @@ ffr_status ffr_create(const char *json, size_t len, const ffr_opts *opts,
                       ffr_ctx **out);
 
 void ffr_destroy(ffr_ctx *ctx);
+
+/* Compile the FFR_KERNEL_JIT kernel of a flame for these options (their
+   precision; the flame's dimensions and colour) ahead of its renders.  Uses
+   NVRTC only: no device is touched, so it can run before a device is
+   chosen, and later contexts of flames with the same structure (the same
+   variation types per xform, whatever their weights, parameters and
+   affines) find the kernel compiled.  FFR_OK also for flames that have no
+   per-flame kernel (FP32, benchmark variations only).  FFR_ERR_PARSE: the
+   flame; FFR_ERR_CUDA: NVRTC missing or the compile failed (message in
+   ffr_last_error(NULL)). */
+ffr_status ffr_jit_prepare(const char *json, size_t len, const ffr_opts *opts);
 
 /* Message of the last failing call on ctx (or of the last failing
    ffr_create on this thread when ctx is NULL).  Never NULL. */

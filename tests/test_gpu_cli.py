@@ -19,15 +19,16 @@ def run(ffr, *args):
     return subprocess.run([ffr.CLI_PATH, *map(str, args)], capture_output=True, timeout=600)
 
 
+@pytest.mark.parametrize("kernel", ["auto", "jit"])
 @pytest.mark.parametrize("name", ["alg2d", "color"])
-def test_ffr_buf_file_equals_oracle(ffr, fo, tmp_path, name):
+def test_ffr_buf_file_equals_oracle(ffr, fo, tmp_path, name, kernel):
     text = golden_flame_text(name)
     f = tmp_path / "flame.json"
     f.write_text(text)
     out = tmp_path / "out.buf"
     S, N, L, seed = 512, 1_000_000, 977, 5
     r = run(ffr, "-f", f, "-o", out, "-s", N, "-b", L, "--streams", S, "--seed", seed,
-            "--settle", 53)
+            "--settle", 53, "--kernel", kernel)
     assert r.returncode == 0, r.stderr.decode()
     err = r.stderr.decode()
     of = fo.OracleFlame(fo.load_flame(text))

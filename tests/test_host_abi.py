@@ -108,7 +108,8 @@ def test_kernel_option_range(ffr):
     raw = json.dumps({"dimensions": 1, "size": [8], "bounds": [[-1, 1]],
                       "xforms": [{"weight": 1, "variations": [{"name": "linear",
                                                                "weight": 1}]}]}).encode()
-    for kernel, rejected in ((-1, True), (4, True), (ffr.KERNEL_HOT, False)):
+    for kernel, rejected in ((-1, True), (5, True), (ffr.KERNEL_HOT, False),
+                             (ffr.KERNEL_JIT, False)):
         o = ffr.Opts()
         lib.ffr_default_opts(ctypes.byref(o))
         o.kernel = kernel
@@ -154,6 +155,8 @@ def test_cli_missing_required(ffr, tmp_path):
 def test_cli_bad_option_value(ffr):
     r = run_cli(ffr, ["-f", "-", "-o", "-", "-s", "abc"])
     assert r.returncode == 1 and b"invalid" in r.stderr
+    r = run_cli(ffr, ["-f", "-", "-o", "-", "-s", "10", "--kernel", "fast"])
+    assert r.returncode == 1 and b"--kernel must be" in r.stderr
 
 
 def test_cli_rejects_bad_flame(ffr, tmp_path):

@@ -1,0 +1,79 @@
+"""The per-flame kernels (FFR_KERNEL_JIT) on the CPU: ffr_jit_prepare runs
+NVRTC without a device, so the generated source of every variation type,
+dimension count, final xform and colour flame is compiled here; the disk
+cache and the argument checks too.  (Their buffers are checked against the
+general kernel on the GPU, test_gpu_jit.py.)"""
+import concurrent.futures as cf
+import glob
+import json
+import os
+
+import jit_cases
+from conftest import golden_flame_text
+
+CASES = jit_cases.cases()
+
+
+def test_cases_cover_every_variation():
+    names = set()
+    for text in CASES.values():
+        for x in json.loads(text)["xforms"]:
+            names.update(v["name"] for v in x["variations"])
+    assert len(names) == 98
+
+
+def test_prepare_compiles_every_case(ffr):
+    """Every case in both precisions (NVRTC compiles them in parallel)."""
+    jobs = [(n, p) for n in sorted(CASES) for p in (ffr.FP64, ffr.FP32)]
+    with cf.ThreadPoolExecutor(max(2, min(len(jobs), os.cpu_count() or 2))) as ex:
+        res = list(ex.map(lambda j: ffr.jit_prepare(CASES[j[0]], j[1]), jobs))
+    bad = [(j, r) for j, r in zip(jobs, res) if r[0] != ffr.FFR_OK]
+    assert not bad, bad[:2]
+
+
+def test_prepare_four_dimensions(ffr):
+    for p in (ffr.FP64, ffr.FP32):
+        st, msg = ffr.jit_prepare(golden_flame_text("d4_mixed"), p)
+        assert st == ffr.FFR_OK, msg
+
+
+def test_disk_cache_and_merged_programs(ffr, flames, tmp_path, monkeypatch):
+    """FFR_JIT_CACHE holds a cubin and its key (the options and the source)
+    per compiled structure; an FP32 flame of the benchmark types has no
+    per-flame kernel (its precompiled merged instantiation runs) and
+    prepares without compiling."""
+    monkeypatch.setenv("FFR_JIT_CACHE", str(tmp_path))
+    text = json.dumps(flames.random_2d(424242, k=5))
+    assert ffr.jit_prepare(text, ffr.FP32)[0] == ffr.FFR_OK
+    assert glob.glob(str(tmp_path / "*")) == []
+    st, msg = ffr.jit_prepare(text, ffr.FP64)
+    assert st == ffr.FFR_OK, msg
+    keys = glob.glob(str(tmp_path / "ffr_*.key"))
+    cubins = glob.glob(str(tmp_path / "ffr_*.cubin"))
+    assert len(keys) == 1 and len(cubins) == 1
+    key = open(keys[0]).read()
+    assert "--fmad=false" in key and "struct FlameSpec" in key
+    assert os.path.getsize(cubins[0]) > 1000
+    # same structure, other weights and affines: the same kernel
+    other = json.loads(text)
+    for x in other["xforms"]:
+        x["weight"] *= 1.5
+        x["pre_affine"]["b"] = [0.25, -0.25]
+    assert ffr.jit_prepare(json.dumps(other), ffr.FP64)[0] == ffr.FFR_OK
+    assert len(glob.glob(str(tmp_path / "ffr_*.key"))) == 1
+
+
+def test_prepare_rejects_bad_input(ffr):
+    st, msg = ffr.jit_prepare("{not json", ffr.FP64)
+    assert st == ffr.FFR_ERR_PARSE
+    st, msg = ffr.jit_prepare(json.dumps({"dimensions": 5, "size": [2] * 5,
+                                          "bounds": [[-1, 1]] * 5, "xforms": []}), ffr.FP64)
+    assert st == ffr.FFR_ERR_PARSE
+    import ctypes
+    lib = ffr.load_library()
+    o = ffr.Opts()
+    lib.ffr_default_opts(ctypes.byref(o))
+    o.abi_version = 1
+    raw = CASES["d1_group0"].encode()
+    assert lib.ffr_jit_prepare(raw, len(raw), ctypes.byref(o)) == ffr.FFR_ERR_ARG
+    assert lib.ffr_jit_prepare(None, 0, None) == ffr.FFR_ERR_ARG
