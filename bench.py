@@ -42,9 +42,10 @@ tv      FP32 against FP64 at a fixed sample count: total-variation distance
         beside the FP64 seed-to-seed noise floor at the same count
 
 --impl reference times that CPU implementation alone, as the reference arm.
---kernel auto|plain|sorted|hot picks the render kernel (default: the
+--kernel auto|plain|sorted|hot|jit picks the render kernel (default: the
 library's autotuner; hot = the plain kernel with the flame's hottest cells
-counted in shared memory) for the default, sierpinski and tetra3d workloads.
+counted in shared memory; jit = the kernel compiled for the flame at run
+time) for the default, sierpinski and tetra3d workloads.
 
 Other configurations (--workload; each prints its own JSON line):
   sierpinski  2-D Sierpinski triangle, 1024x1024, 1e8 samples from 1e6
@@ -468,13 +469,18 @@ def batch256_record(ffr, dev, steps, warmup, with_tv=True, n_tv=8, scale=1.0):
             "clocks": clocks}
 
 
+NO_BAD_LIMIT = 10**15
+
+
 def per_flame_record(ffr, dev, flames, steps=3):
     """The per-flame kernels (KERNEL_JIT, NVRTC) against the general plain
     kernel on flames the precompiled merged instantiations do not cover: a
     random 2-D flame of parameterless variations outside the benchmark
     seven (FP32), and the benchmark flame in the FP64 mirror.  Both kernels
     run the same streams (the plain kernel's default plan), so their
-    buffers must be identical."""
+    buffers must be identical.  No bad-value limit: a render the limit
+    stopped would end early at a time that depends on the race to the stop
+    flag."""
     import numpy as np
     import torch
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -498,19 +504,22 @@ def per_flame_record(ffr, dev, flames, steps=3):
             kw = {} if plan is None else {"streams": plan[0], "traj_len": plan[1]}
             with ffr.BufferRenderer(text, precision=prec, settle=20, device=dev, kernel=kern,
                                     **kw) as r:
-                s = r.render(n, 99)
+                s = r.render(n, 99, bad_limit=NO_BAD_LIMIT)
                 if plan is None:
                     plan = (s.streams, s.traj_len)
                 r.clear()
-                ms, binned = 0.0, 0
+                ms, binned, bad = 0.0, 0, 0
                 for k in range(steps):
                     flush.zero_()
                     torch.cuda.synchronize()
-                    s = r.render(n, 100 + k)
+                    s = r.render(n, 100 + k, bad_limit=NO_BAD_LIMIT)
+                    assert s.ok and s.samples_iterated == n
                     ms += s.kernel_ms
                     binned += s.samples_plotted - s.dropped
+                    bad += s.bad_values
                 rec[kname] = {"value": binned / (ms * 1e-3), "unit": "binned samples/s",
-                              "ms_per_step": ms / steps, "kernel": s.kernel}
+                              "ms_per_step": ms / steps, "kernel": s.kernel,
+                              "bad_values_per_step": bad / steps}
                 counts[kname] = r.counts()
         rec["speedup"] = rec["general"]["ms_per_step"] / rec["per_flame"]["ms_per_step"]
         rec["identical_buffers"] = bool(np.array_equal(counts["general"], counts["per_flame"]))
