@@ -58,6 +58,7 @@ Other configurations (--workload; each prints its own JSON line):
               graph-captured launch per step, FP32
   serving     Poisson request stream (200 req/s for 60 s, seed 23) through
               the serving loop: p50/p99 latency and samples/s
+  perflame    the per_flame_kernels record alone (--steps renders per kernel)
 """
 from __future__ import annotations
 
@@ -528,6 +529,21 @@ def per_flame_record(ffr, dev, flames, steps=3):
     return out
 
 
+def run_perflame(args):
+    """The per-flame kernel record alone (--steps timed renders per kernel)."""
+    got = _setup_single(args)
+    if got is None:
+        return
+    ffr, dev = got
+    recs = per_flame_record(ffr, dev, _flames(), steps=max(1, args.steps))
+    fp32 = recs[0]["per_flame"]
+    _line(args, "per-flame kernels: random 2-D flame of 12 other variations, 1920x1080, "
+          "FP32 (and the benchmark flame, FP64 mirror)", fp32["value"], fp32["ms_per_step"],
+          "f32", {"samples_per_step": recs[0]["samples_per_step"], "settle": 20,
+                  "flush": "256 MiB L2 flush between timed steps"},
+          gpu_launches=2 * len(recs) * (1 + max(1, args.steps)), per_flame_kernels=recs)
+
+
 def run_batch256(args):
     """256 random 2-D flames in one persistent, graph-captured launch per step."""
     got = _setup_single(args)
@@ -723,7 +739,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="random2d",
-                    choices=["random2d", "sierpinski", "tetra3d", "batch256", "serving"])
+                    choices=["random2d", "sierpinski", "tetra3d", "batch256", "serving",
+                             "perflame"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--samples-per-step", type=float, default=1e9)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -749,7 +766,7 @@ def main():
         return
     if args.workload != "random2d":
         {"sierpinski": run_sierpinski, "tetra3d": run_tetra3d, "batch256": run_batch256,
-         "serving": run_serving}[args.workload](args)
+         "serving": run_serving, "perflame": run_perflame}[args.workload](args)
         return
     ws, rank, local = dist_env()
     import torch
