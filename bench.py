@@ -541,7 +541,7 @@ def run_perflame(args):
           "FP32 (and the benchmark flame, FP64 mirror)", fp32["value"], fp32["ms_per_step"],
           "f32", {"samples_per_step": recs[0]["samples_per_step"], "settle": 20,
                   "flush": "256 MiB L2 flush between timed steps"},
-          gpu_launches=2 * len(recs) * (1 + max(1, args.steps)), per_flame_kernels=recs)
+          gpu_launches=2 * len(recs) * max(1, args.steps), per_flame_kernels=recs)
 
 
 def run_batch256(args):
