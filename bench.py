@@ -85,6 +85,8 @@ METRIC = "binned samples/s"
 PORT_VS_REFERENCE = {"threads_8": 3.47, "threads_4": 2.54, "threads_1": 1.07,
                      "host": "x86-64, 8 cores", "script": "oracle/port_vs_reference.py"}
 WORKLOAD = "random 2-D flame, 6 xforms x 2 variations, 1920x1080, 1e10 samples"
+# ffr_stats.kernel -> name
+KERNEL_NAMES = {1: "plain", 2: "xform-sorted", 4: "per-flame", 5: "per-flame xform-sorted"}
 
 
 def dist_env():
@@ -337,14 +339,14 @@ def run_sierpinski(args):
     sampler = ClockSampler(dev)
     sampler.start()
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT, "jit-sorted": ffr.KERNEL_JIT_SORTED}
     for name, prec in (("fp64", ffr.FP64), ("fp32", ffr.FP32)):
         with ffr.BufferRenderer(text, precision=prec, settle=settle, streams=T, traj_len=Lt,
                                 device=dev, kernel=kern[args.kernel]) as r:
             ms, binned, iters, s, n_launch = _timed_steps(r, args, N, 1, flush)
             launches += n_launch
             res[name] = {"value": binned / (ms * 1e-3), "ms_per_step": ms / args.steps,
-                         "kernel": {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel)}
+                         "kernel": KERNEL_NAMES.get(s.kernel)}
             if name == "fp64" and args.verify:
                 r.clear()
                 r.render(N, 1, bad_limit=10**12)
@@ -381,7 +383,7 @@ def run_tetra3d(args):
     text = json.dumps(_flames().tetrahedron_3d((512, 512, 512)))
     B, settle = int(args.samples_per_step), 20
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT, "jit-sorted": ffr.KERNEL_JIT_SORTED}
     with ffr.BufferRenderer(text, precision=ffr.FP32, settle=settle, device=dev,
                             kernel=kern[args.kernel]) as r:
         sampler = ClockSampler(dev)
@@ -404,7 +406,7 @@ def run_tetra3d(args):
     _line(args, "Sierpinski tetrahedron, 512^3 u32 buffer, 1e10 samples", value,
           ms / args.steps, "f32",
           {"samples_per_step": B, "settle": settle, "seed": 3, "streams": s.streams,
-           "traj_len": s.traj_len, "kernel": {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel),
+           "traj_len": s.traj_len, "kernel": KERNEL_NAMES.get(s.kernel),
            "flush": "none: the 512 MiB buffer is larger than L2"},
           gpu_launches=launches,
           roofline={"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -758,7 +760,8 @@ def main():
     ap.add_argument("--serving-seconds", type=float, default=10.0,
                     help="default workload: arrival window of the over-capacity stream "
                          "(the sustainable one runs 1.5x as long)")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "sorted", "hot", "jit"],
+    ap.add_argument("--kernel", default="auto",
+                    choices=["auto", "plain", "sorted", "hot", "jit", "jit-sorted"],
                     help="render kernel (auto: the library's autotuner decides)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -793,7 +796,7 @@ def main():
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     kern = {"auto": ffr.KERNEL_AUTO, "plain": ffr.KERNEL_PLAIN, "sorted": ffr.KERNEL_SORTED,
-            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT}
+            "hot": ffr.KERNEL_HOT, "jit": ffr.KERNEL_JIT, "jit-sorted": ffr.KERNEL_JIT_SORTED}
     r = ffr.BufferRenderer(text, precision=prec, settle=settle, device=local,
                            kernel=kern[args.kernel])
     for w in range(args.warmup):
@@ -815,7 +818,7 @@ def main():
         iters += s.samples_iterated
         launches += 1 + s.aux_launches
         streams, traj_len = s.streams, s.traj_len
-        kernel_used = {1: "plain", 2: "xform-sorted", 4: "per-flame"}.get(s.kernel) + (
+        kernel_used = KERNEL_NAMES.get(s.kernel) + (
             " + warp-merged bins" if s.agg else "") + (
             f" + {s.hot_cells} hot cells in shared memory" if s.hot_cells else "")
     barrier()

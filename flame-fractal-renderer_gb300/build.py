@@ -62,7 +62,7 @@ def _run(cmd: list[str]) -> None:
 # headers the per-flame kernels (csrc/jit.cpp, NVRTC) include, embedded in
 # the library so that it needs no source tree at run time
 JIT_HEADERS = ["std_types.h", "variation_ids.h", "flame_program.h", "isaac64.cuh", "launch.h",
-               "variations.cuh", "chaos_kernel.cuh"]
+               "variations.cuh", "chaos_kernel.cuh", "chaos_sorted.cuh"]
 JIT_INC = os.path.join(OUT, "jit_headers.inc")
 
 

@@ -151,6 +151,8 @@ struct ffr_ctx
     // none (the FP32 merged form)
     const JitKernel* jit = nullptr;
     std::string jit_source;
+    const JitKernel* jit_sorted = nullptr;      // the xform-sorted per-flame kernel
+    std::string jit_sorted_source;
     // kernels launched by the current call besides the render kernel
     unsigned int aux_launches = 0;
     std::string err = "no error";
@@ -332,17 +334,20 @@ int program_words(const ffr_ctx* c)
     return (int)h->rng_words_max;       // same offset in the float header
 }
 
-// The per-flame kernel of the context's program, compiled on first use (or
-// found in the caches); ready_only: only if no compile is needed
-ffr_status ensure_jit(ffr_ctx* c, bool ready_only = false)
+// A per-flame kernel of the context's program (the plain one, or with
+// sorted the xform-sorted one), compiled on first use (or found in the
+// caches); ready_only: only if no compile is needed
+ffr_status ensure_jit(ffr_ctx* c, bool sorted, bool ready_only = false)
 {
-    if (c->jit)
+    const JitKernel*& k = sorted ? c->jit_sorted : c->jit;
+    if (k)
         return FFR_OK;
-    if (c->jit_source.empty())
-        c->jit_source = jit_source(c->prog_host, c->opts.precision, c->flame.color_dims > 0);
+    std::string& src = sorted ? c->jit_sorted_source : c->jit_source;
+    if (src.empty())
+        src = jit_source(c->prog_host, c->opts.precision, c->flame.color_dims > 0, sorted);
     std::string err;
-    c->jit = jit_kernel(c->jit_source, c->opts.precision, &err, !ready_only);
-    if (!c->jit)
+    k = jit_kernel(src, c->opts.precision, &err, !ready_only);
+    if (!k)
         return ready_only ? FFR_ERR_ARG : fail(c, FFR_ERR_CUDA, err);
     return FFR_OK;
 }
@@ -367,20 +372,21 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
     const unsigned int pb = prog_smem_for(c->prog_host.data());
     const int nxf = (int)c->flame.xforms.size();
     int k = kreq;
-    if (k == FFR_KERNEL_JIT)
+    // programs in the FP32 merged form have no per-flame kernel: their
+    // precompiled instantiation already runs without type dispatch
+    if ((k == FFR_KERNEL_JIT || k == FFR_KERNEL_JIT_SORTED) && merged_for(c->prog_host.data()))
+        k = FFR_KERNEL_PLAIN;
+    if (k == FFR_KERNEL_JIT_SORTED && (c->flame.dims > 3 || nxf > kSortedMaxXforms))
+        return fail(c, FFR_ERR_ARG, "per-flame xform-sorted kernel cannot run this flame "
+            "(more than 3 dims or 16 xforms)");
+    if (k == FFR_KERNEL_JIT || k == FFR_KERNEL_JIT_SORTED)
     {
-        // programs in the FP32 merged form have no per-flame kernel: their
-        // precompiled instantiation already runs without type dispatch
-        if (merged_for(c->prog_host.data()))
-            k = FFR_KERNEL_PLAIN;
-        else
-        {
-            ffr_status js = ensure_jit(c);
-            if (js != FFR_OK)
-                return js;
-        }
+        ffr_status js = ensure_jit(c, k == FFR_KERNEL_JIT_SORTED);
+        if (js != FFR_OK)
+            return js;
     }
-    if (k != FFR_KERNEL_PLAIN && k != FFR_KERNEL_JIT && !c->L().occ_sorted)
+    const bool jit_k = k == FFR_KERNEL_JIT || k == FFR_KERNEL_JIT_SORTED;
+    if (k != FFR_KERNEL_PLAIN && !jit_k && !c->L().occ_sorted)
     {
         // no xform-sorted instantiation for this dimension count
         if (k == FFR_KERNEL_SORTED)
@@ -388,7 +394,7 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
                 "(dims " + std::to_string(c->flame.dims) + ": plain kernel only)");
         k = FFR_KERNEL_PLAIN;
     }
-    if (k != FFR_KERNEL_PLAIN && k != FFR_KERNEL_JIT)
+    if (k != FFR_KERNEL_PLAIN && !jit_k)
     {
         CU(c, c->L().occ_sorted(color, spill, &bps, &block, pb, nxf, program_words(c), &smem));
         if (bps >= 1)
@@ -409,6 +415,16 @@ ffr_status plan(ffr_ctx* c, uint64_t samples, int kreq, uint64_t* streams, uint6
         block = kJitBlock;
         smem = chaos_smem_bytes<kJitBlock>(pb, nxf, rsl_words_for(c->prog_host.data()), use_hot);
         CU(c, jit_occupancy(c->jit, smem, &bps));
+    }
+    else if (k == FFR_KERNEL_JIT_SORTED)
+    {
+        block = kSortedBlock;
+        smem = sorted_smem_bytes<kSortedBlock>(pb, nxf, program_words(c), c->flame.dims,
+                                               c->opts.precision == FFR_FP64 ? 8 : 4);
+        CU(c, jit_occupancy(c->jit_sorted, smem, &bps));
+        if (bps < 1)
+            return fail(c, FFR_ERR_ARG, "per-flame xform-sorted kernel cannot run this flame "
+                "(not enough shared memory)");
     }
     *kernel = k;
     if (bps < 1)
@@ -511,6 +527,12 @@ cudaError_t launch_render_kernel(ffr_ctx* c, int kernel, const RenderArgs& a, in
         return jit_launch(c->jit, a, grid,
                           chaos_smem_bytes<kJitBlock>(a.prog_bytes, a.nxf, a.rsl_words,
                                                       a.hot_keys != nullptr),
+                          c->stream);
+    if (kernel == FFR_KERNEL_JIT_SORTED)
+        return jit_launch(c->jit_sorted, a, grid,
+                          sorted_smem_bytes<kSortedBlock>(a.prog_bytes, a.nxf, a.rng_words,
+                                                          c->flame.dims,
+                                                          c->opts.precision == FFR_FP64 ? 8 : 4),
                           c->stream);
     return c->L().render(a, grid, c->stream);
 }
@@ -834,10 +856,18 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     // the per-flame kernel is a candidate when it is compiled already (an
     // earlier FFR_KERNEL_JIT render or ffr_jit_prepare, in this process or
     // in the FFR_JIT_CACHE directory): the autotuner never waits for NVRTC
-    const bool jit_ready = !merged_for(c->prog_host.data()) && ensure_jit(c, true) == FFR_OK;
-    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED, FFR_KERNEL_JIT})
+    const bool merged = merged_for(c->prog_host.data()) != 0;
+    const bool jit_ready = !merged && ensure_jit(c, false, true) == FFR_OK;
+    const bool jit_sorted_ready = !merged && c->flame.dims <= 3
+        && c->flame.xforms.size() <= (size_t)kSortedMaxXforms
+        && ensure_jit(c, true, true) == FFR_OK;
+    auto ready = [&](int k) {
+        return k == FFR_KERNEL_JIT ? jit_ready : k == FFR_KERNEL_JIT_SORTED ? jit_sorted_ready
+                                                                           : true;
+    };
+    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED, FFR_KERNEL_JIT, FFR_KERNEL_JIT_SORTED})
         for (int g : {0, 1})
-            if (st == FFR_OK && (k != FFR_KERNEL_JIT || jit_ready))
+            if (st == FFR_OK && ready(k))
                 st = probe(k, g, false);
     // the probes' counts (u32: far below 2^32 per cell) locate hot cells
     unsigned int mult = 0;
@@ -849,7 +879,7 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     if (st == FFR_OK && mult)
         for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_JIT})
             for (int g : {0, 1})
-                if (st == FFR_OK && (k != FFR_KERNEL_JIT || jit_ready))
+                if (st == FFR_OK && ready(k))
                     st = probe(k, g, true);
     // launch shape for the best candidate: fewer resident CTAs per SM, each
     // thread then running more streams one after another (the streams, and
@@ -944,7 +974,7 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: ABI version mismatch");
     if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown precision");
-    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_JIT)
+    if (o.kernel < FFR_KERNEL_AUTO || o.kernel > FFR_KERNEL_JIT_SORTED)
         return fail(nullptr, FFR_ERR_ARG, "ffr_create: unknown kernel");
     ffr_ctx* c = new (std::nothrow) ffr_ctx;
     if (!c)
@@ -1044,23 +1074,30 @@ ffr_status ffr_jit_prepare(const char* json, size_t len, const ffr_opts* opts)
         return fail(nullptr, FFR_ERR_ARG, "ffr_jit_prepare: ABI version mismatch");
     if (o.precision != FFR_FP64 && o.precision != FFR_FP32)
         return fail(nullptr, FFR_ERR_ARG, "ffr_jit_prepare: unknown precision");
-    std::string src;
+    // the per-flame kernels asked for: plain (FFR_KERNEL_JIT), xform-sorted
+    // (FFR_KERNEL_JIT_SORTED), or both (any other kernel value)
+    std::vector<std::string> srcs;
     try
     {
         const HostFlame f = parse_flame(std::string(json, len));
         const std::vector<uint8_t> prog = o.precision == FFR_FP64 ? build_program<double>(f)
                                                                   : build_program<float>(f);
-        src = jit_source(prog, o.precision, f.color_dims > 0);
+        for (bool sorted : {false, true})
+            if (o.kernel != (sorted ? FFR_KERNEL_JIT : FFR_KERNEL_JIT_SORTED))
+                srcs.push_back(jit_source(prog, o.precision, f.color_dims > 0, sorted));
     }
     catch (const std::exception& e)
     {
         return fail(nullptr, FFR_ERR_PARSE, e.what());
     }
-    if (src.empty())
-        return FFR_OK;      // FP32 merged form: no per-flame kernel
-    std::string err;
-    if (!jit_compile_only(src, o.precision, &err))
-        return fail(nullptr, FFR_ERR_CUDA, err);
+    for (const std::string& src : srcs)
+    {
+        if (src.empty())
+            continue;       // FP32 merged form, or no sorted kernel for the flame
+        std::string err;
+        if (!jit_compile_only(src, o.precision, &err))
+            return fail(nullptr, FFR_ERR_CUDA, err);
+    }
     return FFR_OK;
 }
 

@@ -275,8 +275,6 @@ cudaError_t FFR_NAME(launch_trace)(const TraceArgs& a, cudaStream_t st)
 
 #elif FFR_KIND == 1
 
-constexpr int kSortedBlock = 256;
-
 template <bool C>
 static cudaError_t launch_sorted_one(const RenderArgs& a, int grid, cudaStream_t st)
 {

@@ -355,6 +355,87 @@ __device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT
     }
 }
 
+// Per-xform code for kernels whose warps apply one xform at a time (the
+// xform-sorted kernel's chunks, the final xform): XForm::applyIteration for
+// an xform known at compile time, its variations from pg.var[K] on with
+// types TYPES... in order; PRESENT = the kTa* bits of its own types (the
+// plane primitives it needs; the variation results do not depend on which
+// other types share them); PRE / POST: it has the affine (used above 2
+// dims only, as in apply_xform).  The arithmetic is apply_xform's general
+// path on the same program data.
+template <int D, typename R, uint32_t PRESENT, int K, int... TYPES>
+struct FixedVars
+{
+    template <typename Rng>
+    __device__ static __forceinline__ void run(const Prog<R>&, const R*, R*, Rng&,
+                                               const PlanePrims<R>&)
+    {
+    }
+};
+
+template <int D, typename R, uint32_t PRESENT, int K, int T0, int... REST>
+struct FixedVars<D, R, PRESENT, K, T0, REST...>
+{
+    template <typename Rng>
+    __device__ static __forceinline__ void run(const Prog<R>& pg, const R* t, R* v, Rng& rng,
+                                               const PlanePrims<R>& pp)
+    {
+        const VarT<R>& var = pg.var[K];
+        R o[D];
+        variation<D, R, T0>(var, t, o, rng, PRESENT, pp);
+        const R w = var.weight;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] += o[i] * w;
+        FixedVars<D, R, PRESENT, K + 1, REST...>::run(pg, t, v, rng, pp);
+    }
+};
+
+template <int D, typename R, uint32_t PRESENT, bool PRE, bool POST, int K, int... TYPES>
+struct FixedXform
+{
+    template <typename Rng>
+    __device__ static __forceinline__ void apply(const Prog<R>& pg, const XformT<R>& x,
+                                                 const R* p, R* out, Rng& rng)
+    {
+        R t[D], v[D];
+        if (D < 3 || PRE)
+            affine<D>(x.pre, p, t);
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                t[i] = p[i];
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            v[i] = R(0);
+        PlanePrims<R> pp;
+        pp.valid = false;
+        pp.q = pp.rt = pp.ang = R(0);
+        if constexpr (D == 2 && (PRESENT & (kTaSwirl | kTaHorseshoe | kTaPolar | kTaJulia)))
+        {
+            using T = RealTraits<R>;
+            const R px = t[0], py = t[D - 1];
+            pp.valid = true;
+            pp.q = px * px + py * py;
+            if (PRESENT & (kTaHorseshoe | kTaPolar | kTaJulia))
+                pp.rt = T::sqrt_(pp.q);
+            if (PRESENT & (kTaPolar | kTaJulia))
+                pp.ang = T::atan2_(py, px);
+        }
+        FixedVars<D, R, PRESENT, K, TYPES...>::run(pg, t, v, rng, pp);
+        if (D < 3 || POST)
+            affine<D>(x.post, v, out);
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                out[i] = v[i];
+        }
+    }
+};
+
 // one xform application in the render loop: the flame's own code (SP), or
 // apply_xform
 template <int D, typename R, int VS, typename SP, typename Rng>

@@ -36,27 +36,6 @@
 
 namespace ffr {
 
-// xforms a sorted CTA handles (per-xform lists and counters in shared memory)
-constexpr int kSortedMaxXforms = 16;
-constexpr int kRslWords = 24;          // 16 fresh words + carried tail
-constexpr int kMaxRefillLow = kRslWords - 16;
-
-template <int T>
-__host__ __device__ inline size_t sorted_smem_bytes(unsigned int prog_bytes, int nxf,
-                                                    int words, int dims, int real_bytes)
-{
-    size_t s = align16u(prog_bytes);
-    s += (16 + kRslWords + 3) * (size_t)T * 8;            // ISAAC state
-    s += (size_t)words * T * 8;                           // pre-drawn words [W][T]
-    s += (((size_t)dims * T * real_bytes) + 15) & ~(size_t)15;   // staged points [D][T]
-    s += (((size_t)nxf * T * 4) + 15) & ~(size_t)15;      // per-thread xform counts
-    s += (((size_t)nxf * T * 2) + 15) & ~(size_t)15;      // per-xform lists (u16)
-    s += (((size_t)T * 2) + 15) & ~(size_t)15;            // refill list (u16)
-    s += (((size_t)T) + 15) & ~(size_t)15;                // words left at refill (u8)
-    s += (2 * kSortedMaxXforms + 2) * 4;                  // list counters x2
-    return s;
-}
-
 // ISAAC state of one stream in shared memory, stride T
 template <int T>
 struct SmemIsaac
@@ -145,7 +124,20 @@ struct PreDrawn
     __device__ __forceinline__ uint64_t next() { return w[(k++) * T]; }
 };
 
-template <int D, typename R, bool COLOR, int T>
+// One xform application by a warp that applies xform xi on every lane (a
+// chunk of phase B, the final xform): the flame's per-xform code (SP, a
+// per-flame kernel), or apply_xform
+template <int D, typename R, typename SP, typename Rng>
+__device__ __forceinline__ void sorted_xform(const Prog<R>& pg, int xi, const R* p, R* out,
+                                             Rng& rng)
+{
+    if constexpr (SP::on)
+        SP::template xform<D, R>(pg, xi, p, out, rng);
+    else
+        apply_xform<D, R>(pg, pg.xf[xi], p, out, rng);
+}
+
+template <int D, typename R, bool COLOR, int T, typename SP = NoSpec>
 __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* smem)
 {
     using Tr = RealTraits<R>;
@@ -407,7 +399,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
                 for (int d = 0; d < D; ++d)
                     pin[d] = stage[d * T + o];
                 PreDrawn<T> pw{words + o, 0};
-                apply_xform<D, R>(pg, pg.xf[i], pin, pout, pw);
+                sorted_xform<D, R, SP>(pg, i, pin, pout, pw);
 #pragma unroll
                 for (int d = 0; d < D; ++d)
                     stage[d * T + o] = pout[d];
@@ -452,7 +444,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             if (h.has_final)
             {
                 const XformT<R>& ff = pg.xf[nxf];
-                apply_xform<D, R>(pg, ff, p, pf, rng);
+                sorted_xform<D, R, SP>(pg, nxf, p, pf, rng);
                 if (COLOR)
                 {
                     if (ff.has_color)

@@ -26,8 +26,9 @@
 // (default 53 = settle_iters<double>), --streams N, --trajectories T (T
 // streams of one trajectory each, of ceil(samples / T) samples: "N samples
 // from T trajectories"; excludes -b and --streams), --device N,
-// --timeout-ms N, --kernel auto|plain|sorted|hot|jit (ffr_opts.kernel; jit =
-// the kernel compiled for this flame's structure at run time).
+// --timeout-ms N, --kernel auto|plain|sorted|hot|jit|jit-sorted
+// (ffr_opts.kernel; jit, jit-sorted = the plain and xform-sorted kernels
+// compiled for this flame's structure at run time).
 //
 // Errors: the reference lets parse/IO exceptions escape main (abort); this
 // front end prints "ERROR: <message>" and exits 1.  A bad-value stop prints
@@ -89,7 +90,7 @@ const char* kUsage =
     "  --trajectories arg            trajectories (one stream each)\n"
     "  --device arg (=0)             CUDA device\n"
     "  --timeout-ms arg (=0)         render time limit (0 = none)\n"
-    "  --kernel arg (=auto)          auto, plain, sorted, hot or jit\n";
+    "  --kernel arg (=auto)          auto, plain, sorted, hot, jit or jit-sorted\n";
 
 [[noreturn]] void die(const std::string& m)
 {
@@ -188,15 +189,16 @@ Args parse_args(int argc, char** argv)
         else if (n == "timeout-ms") a.timeout_ms = to_u64(val, n);
         else if (n == "kernel")
         {
-            static_assert(FFR_KERNEL_AUTO == 0 && FFR_KERNEL_JIT == 4, "kernel names");
-            static const char* const kNames[] = {"auto", "plain", "sorted", "hot", "jit"};
+            static_assert(FFR_KERNEL_AUTO == 0 && FFR_KERNEL_JIT_SORTED == 5, "kernel names");
+            static const char* const kNames[] = {"auto", "plain", "sorted", "hot", "jit",
+                                                 "jit-sorted"};
             int k = -1;
-            for (int i = 0; i < 5; ++i)
+            for (int i = 0; i < 6; ++i)
                 if (val == kNames[i])
                     k = i;
             if (k < 0)
-                die("--kernel must be auto, plain, sorted, hot or jit");
-            a.kernel = k;       // FFR_KERNEL_AUTO .. FFR_KERNEL_JIT in this order
+                die("--kernel must be auto, plain, sorted, hot, jit or jit-sorted");
+            a.kernel = k;       // FFR_KERNEL_AUTO .. FFR_KERNEL_JIT_SORTED in this order
         }
     }
     return a;

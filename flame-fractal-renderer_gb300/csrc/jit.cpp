@@ -47,27 +47,34 @@ int tier_a_type(int bit)
 }
 
 template <typename R>
-std::string source_for(const std::vector<unsigned char>& prog, int precision, bool color)
+std::string source_for(const std::vector<unsigned char>& prog, int precision, bool color,
+                       bool sorted)
 {
     ProgHeader<R> h;
     if (prog.size() < sizeof h)
         return std::string();
     std::memcpy(&h, prog.data(), sizeof h);
-    if (h.merged)
+    if (h.merged || (sorted && (h.dims > 3 || h.nxf > kSortedMaxXforms)))
         return std::string();
     // the types each variation slot holds over the selectable and final xforms
     const int nx = h.nxf + (h.has_final ? 1 : 0);
     std::vector<uint32_t> ta;               // kTa* bits per slot
     std::vector<std::set<int>> other;       // the other types per slot
+    std::ostringstream per_xform;           // the cases of FlameSpec::xform
     for (int i = 0; i < nx; ++i)
     {
         XformT<R> x;
         std::memcpy(&x, prog.data() + h.off_xf + (size_t)i * sizeof x, sizeof x);
+        uint32_t xpresent = 0;
+        std::string xtypes, xnames;
         for (int k = 0; k < x.var_count; ++k)
         {
             VarT<R> v;
             std::memcpy(&v, prog.data() + h.off_var + (size_t)(x.var_begin + k) * sizeof v,
                         sizeof v);
+            xpresent |= tier_a_bit(v.type);
+            xtypes += ", " + std::to_string(v.type);
+            xnames += std::string(xnames.empty() ? "" : " ") + variation_name(v.type);
             if ((int)ta.size() <= k)
             {
                 ta.resize(k + 1, 0u);
@@ -78,12 +85,20 @@ std::string source_for(const std::vector<unsigned char>& prog, int precision, bo
             else
                 other[k].insert(v.type);
         }
+        per_xform << "        " << (i + 1 == nx ? std::string("default")
+                                                 : "case " + std::to_string(i))
+                  << ":   // " << (i == h.nxf ? "final" : "xform " + std::to_string(i))
+                  << ": " << (xnames.empty() ? "no variations" : xnames) << "\n"
+                  << "            FixedXform<D, R, " << xpresent << "u, "
+                  << (x.has_pre ? "true" : "false") << ", " << (x.has_post ? "true" : "false")
+                  << ", " << x.var_begin << xtypes << ">::apply(pg, pg.xf[" << i
+                  << "], p, out, rng);\n            return;\n";
     }
     std::ostringstream s;
     s << "// per-flame render kernel (" << h.dims << " dims, "
       << (precision ? "FP32" : "FP64") << (color ? ", colour" : "") << ", " << h.nxf
       << " xforms" << (h.has_final ? " + final" : "") << ")\n"
-      << "#include \"chaos_kernel.cuh\"\n"
+      << (sorted ? "#include \"chaos_sorted.cuh\"\n" : "#include \"chaos_kernel.cuh\"\n")
       << "namespace ffr {\n"
       << "struct FlameSpec\n{\n"
       << "    static constexpr bool on = true;\n"
@@ -107,8 +122,27 @@ std::string source_for(const std::vector<unsigned char>& prog, int precision, bo
           << "\n            SlotTypes<D, R, " << ta[k] << "u" << types
           << ">::eval(var, t, o, rng, pp);\n";
     }
-    s << "    }\n};\n} // namespace ffr\n\n"
-      << "extern \"C\" __global__ void __launch_bounds__(" << kJitBlock << ", "
+    s << "    }\n";
+    if (sorted)
+        s << "    // warps that apply one xform on every lane (sorted chunks, final xform)\n"
+          << "    template <int D, typename R, typename Rng>\n"
+          << "    __device__ static __forceinline__ void xform(const Prog<R>& pg, int xi, "
+             "const R* p, R* out, Rng& rng)\n    {\n        switch (xi)\n        {\n"
+          << per_xform.str() << "        }\n    }\n";
+    s << "};\n} // namespace ffr\n\n";
+    if (sorted)
+    {
+        s << "extern \"C\" __global__ void __launch_bounds__(" << kSortedBlock << ", 2)\n"
+          << "ffr_flame_sorted(const ffr::RenderArgs a)\n{\n"
+          << "    extern __shared__ __align__(16) unsigned char smem[];\n"
+          << "    ffr::load_program<" << kSortedBlock << ">(smem, a.prog, a.prog_bytes);\n"
+          << "    __syncthreads();\n"
+          << "    ffr::sorted_body<" << h.dims << ", " << (precision ? "float" : "double")
+          << ", " << (color ? "true" : "false") << ", " << kSortedBlock
+          << ", ffr::FlameSpec>(a, smem);\n}\n";
+        return s.str();
+    }
+    s << "extern \"C\" __global__ void __launch_bounds__(" << kJitBlock << ", "
       << "ffr::render_min_blocks<" << (precision ? "float" : "double") << ">())\n"
       << "ffr_flame_render(const ffr::RenderArgs a)\n{\n"
       << "    extern __shared__ __align__(16) unsigned char smem[];\n"
@@ -347,10 +381,11 @@ Entry* entry_for(const std::string& src, int precision, std::string* err, bool c
 
 } // namespace
 
-std::string jit_source(const std::vector<unsigned char>& prog, int precision, bool color)
+std::string jit_source(const std::vector<unsigned char>& prog, int precision, bool color,
+                       bool sorted)
 {
-    return precision == 0 ? source_for<double>(prog, 0, color)
-                          : source_for<float>(prog, 1, color);
+    return precision == 0 ? source_for<double>(prog, 0, color, sorted)
+                          : source_for<float>(prog, 1, color, sorted);
 }
 
 bool jit_compile_only(const std::string& source, int precision, std::string* err)
@@ -366,6 +401,8 @@ bool jit_compile_only(const std::string& source, int precision, std::string* err
 const JitKernel* jit_kernel(const std::string& source, int precision, std::string* err,
                             bool compile)
 {
+    // the entry point the source defines
+    const bool sorted = source.find("ffr_flame_sorted(") != std::string::npos;
     if (source.empty())
     {
         *err = "no per-flame kernel for this program";
@@ -382,7 +419,8 @@ const JitKernel* jit_kernel(const std::string& source, int precision, std::strin
                                          nullptr, nullptr, 0);
     if (ce == cudaSuccess)
     {
-        ce = cudaLibraryGetKernel(&k->kernel, k->lib, "ffr_flame_render");
+        ce = cudaLibraryGetKernel(&k->kernel, k->lib,
+                                  sorted ? "ffr_flame_sorted" : "ffr_flame_render");
         if (ce != cudaSuccess)
             cudaLibraryUnload(k->lib);
     }
@@ -398,6 +436,7 @@ const JitKernel* jit_kernel(const std::string& source, int precision, std::strin
         k->local_bytes = (int)fa.localSizeBytes;
     }
     k->compile_ms = e->compile_ms;
+    k->block = sorted ? kSortedBlock : kJitBlock;
     e->loaded = std::move(k);
     return e->loaded.get();
 }
@@ -409,7 +448,7 @@ cudaError_t jit_occupancy(const JitKernel* k, size_t smem, int* blocks_per_sm)
                                          (int)smem);
     if (e != cudaSuccess)
         return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kJitBlock, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, k->block, smem);
 }
 
 cudaError_t jit_launch(const JitKernel* k, const RenderArgs& a, int grid, size_t smem,
@@ -422,7 +461,7 @@ cudaError_t jit_launch(const JitKernel* k, const RenderArgs& a, int grid, size_t
         return e;
     RenderArgs copy = a;
     void* params[] = {&copy};
-    return cudaLaunchKernel(f, dim3((unsigned)grid), dim3(kJitBlock), params, smem, st);
+    return cudaLaunchKernel(f, dim3((unsigned)grid), dim3((unsigned)k->block), params, smem, st);
 }
 
 } // namespace ffr

@@ -29,16 +29,23 @@ struct JitKernel
 {
     cudaLibrary_t lib;
     cudaKernel_t kernel;
+    int block;              // threads per CTA
     int regs;               // registers per thread
     int local_bytes;        // local memory (stack, spills) per thread
     double compile_ms;      // NVRTC time (0 when loaded from the disk cache)
 };
 
 // The per-flame render kernel's source for a program blob (ProgHeader<R>
-// first; precision 0 = FP64, 1 = FP32), with or without colour.  Empty for
-// programs in the FP32 merged form, which the precompiled merged
-// instantiations already run without dispatch.
-std::string jit_source(const std::vector<unsigned char>& prog, int precision, bool color);
+// first; precision 0 = FP64, 1 = FP32), with or without colour: the plain
+// kernel (entry ffr_flame_render, each variation slot's dispatch narrowed
+// to the slot's types) or, with sorted, the xform-sorted kernel (entry
+// ffr_flame_sorted, whose warps apply one xform at a time, each xform's
+// code with its types fixed).  Empty for programs in the FP32 merged form,
+// which the precompiled merged instantiations already run without dispatch,
+// and for sorted kernels of flames the sorted kernel does not take (above 3
+// dims or kSortedMaxXforms xforms).
+std::string jit_source(const std::vector<unsigned char>& prog, int precision, bool color,
+                       bool sorted = false);
 
 // The loaded kernel for a source (compiled on first use; with compile
 // false, only if the process or the disk cache already holds it); null and
@@ -54,7 +61,8 @@ cudaError_t jit_occupancy(const JitKernel* k, size_t smem, int* blocks_per_sm);
 cudaError_t jit_launch(const JitKernel* k, const RenderArgs& a, int grid, size_t smem,
                        cudaStream_t st);
 
-// threads per CTA of the per-flame kernels
+// threads per CTA of the per-flame plain kernels (the sorted ones:
+// kSortedBlock)
 constexpr int kJitBlock = 128;
 
 } // namespace ffr

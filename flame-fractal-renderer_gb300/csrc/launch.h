@@ -223,6 +223,30 @@ __host__ __device__ inline size_t chaos_smem_bytes(unsigned int prog_bytes, int 
     return s;
 }
 
+// The xform-sorted render kernel (chaos_sorted.cuh): threads per CTA, the
+// xforms a CTA handles (per-xform lists and counters in shared memory), its
+// ISAAC result array and dynamic shared memory
+constexpr int kSortedBlock = 256;
+constexpr int kSortedMaxXforms = 16;
+constexpr int kRslWords = 24;          // 16 fresh words + carried tail
+constexpr int kMaxRefillLow = kRslWords - 16;
+
+template <int T>
+__host__ __device__ inline size_t sorted_smem_bytes(unsigned int prog_bytes, int nxf,
+                                                    int words, int dims, int real_bytes)
+{
+    size_t s = align16u(prog_bytes);
+    s += (16 + kRslWords + 3) * (size_t)T * 8;            // ISAAC state
+    s += (size_t)words * T * 8;                           // pre-drawn words [W][T]
+    s += (((size_t)dims * T * real_bytes) + 15) & ~(size_t)15;   // staged points [D][T]
+    s += (((size_t)nxf * T * 4) + 15) & ~(size_t)15;      // per-thread xform counts
+    s += (((size_t)nxf * T * 2) + 15) & ~(size_t)15;      // per-xform lists (u16)
+    s += (((size_t)T * 2) + 15) & ~(size_t)15;            // refill list (u16)
+    s += (((size_t)T) + 15) & ~(size_t)15;                // words left at refill (u8)
+    s += (2 * kSortedMaxXforms + 2) * 4;                  // list counters x2
+    return s;
+}
+
 // One job of a batched launch: the arguments ffr_render would use for the
 // context alone, and its range of chunks (BLOCK streams each) in the
 // batch's chunk order.  The launch runs the job's chunks chunk_first ..

@@ -31,7 +31,8 @@ STATUS_NAMES = ["FFR_OK", "FFR_BAD_VALUES", "FFR_ERR_PARSE", "FFR_ERR_ARG",
                 "FFR_ERR_IO", "FFR_ERR_OOM", "FFR_ERR_TIMEOUT", "FFR_ERR_CUDA",
                 "FFR_ERR_STATE"]
 FP64, FP32 = 0, 1
-KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED, KERNEL_HOT, KERNEL_JIT = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_SORTED, KERNEL_HOT, KERNEL_JIT, KERNEL_JIT_SORTED = (
+    0, 1, 2, 3, 4, 5)
 
 # every symbol include/ffr_gpu.h declares
 EXPORTS = [
@@ -414,14 +415,16 @@ def create_status(flame_text: str, precision: int = FP64):
     return st, msg
 
 
-def jit_prepare(flame_text: str, precision: int = FP64):
+def jit_prepare(flame_text: str, precision: int = FP64, kernel: int = KERNEL_AUTO):
     """(status, message) of ffr_jit_prepare: compile the flame's per-flame
-    kernel (KERNEL_JIT) with NVRTC, without a device."""
+    kernels with NVRTC, without a device (kernel KERNEL_JIT or
+    KERNEL_JIT_SORTED: that one; otherwise both)."""
     lib = load_library()
     raw = flame_text.encode("utf-8")
     o = Opts()
     lib.ffr_default_opts(ctypes.byref(o))
     o.precision = precision
+    o.kernel = kernel
     st = lib.ffr_jit_prepare(raw, len(raw), ctypes.byref(o))
     return st, lib.ffr_last_error(None).decode("utf-8", "replace")
 

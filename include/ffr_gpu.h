@@ -99,11 +99,13 @@ typedef struct ffr_opts {
    needs it unless ffr_jit_prepare compiled it, cached per process and, with
    FFR_JIT_CACHE naming a directory, on disk; FP32 programs of the seven
    benchmark variations run their precompiled merged instantiation instead
-   (stats.kernel PLAIN).  AUTO also times the JIT kernel when it is already
-   compiled.  All choices give identical buffers for equal streams and
-   trajectory lengths. */
+   (stats.kernel PLAIN).  JIT_SORTED: the xform-sorted kernel compiled the
+   same way, its warps running each xform's own code (flames of 1..3 dims and
+   at most 16 xforms).  AUTO also times the per-flame kernels when they are
+   already compiled.  All choices give identical buffers for equal streams
+   and trajectory lengths. */
 enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2, FFR_KERNEL_HOT = 3,
-       FFR_KERNEL_JIT = 4 };
+       FFR_KERNEL_JIT = 4, FFR_KERNEL_JIT_SORTED = 5 };
 
 typedef struct ffr_stats {
     uint64_t samples_iterated;   /* getSamplesIterated */
@@ -123,7 +125,7 @@ typedef struct ffr_stats {
     uint64_t traj_len;
     uint64_t settle;
     double kernel_ms;            /* device time of the render kernel(s) */
-    int32_t kernel;              /* FFR_KERNEL_PLAIN, _SORTED or _JIT */
+    int32_t kernel;              /* FFR_KERNEL_PLAIN, _SORTED, _JIT or _JIT_SORTED */
     int32_t agg;                 /* 1: equal-cell increments were warp-merged */
     int32_t hot_cells;           /* cells counted in per-CTA shared memory
                                     (the autotuner's hot-cell table), or 0 */
@@ -154,8 +156,10 @@ ffr_status ffr_create(const char *json, size_t len, const ffr_opts *opts,
 
 void ffr_destroy(ffr_ctx *ctx);
 
-/* Compile the FFR_KERNEL_JIT kernel of a flame for these options (their
-   precision; the flame's dimensions and colour) ahead of its renders.  Uses
+/* Compile the per-flame kernels of a flame for these options (their
+   precision; the flame's dimensions and colour) ahead of its renders:
+   opts->kernel FFR_KERNEL_JIT or FFR_KERNEL_JIT_SORTED compiles that one,
+   any other value both (the sorted one where the flame allows it).  Uses
    NVRTC only: no device is touched, so it can run before a device is
    chosen, and later contexts of flames with the same structure (the same
    variation types per xform, whatever their weights, parameters and

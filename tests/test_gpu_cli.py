@@ -19,7 +19,7 @@ def run(ffr, *args):
     return subprocess.run([ffr.CLI_PATH, *map(str, args)], capture_output=True, timeout=600)
 
 
-@pytest.mark.parametrize("kernel", ["auto", "jit"])
+@pytest.mark.parametrize("kernel", ["auto", "jit", "jit-sorted"])
 @pytest.mark.parametrize("name", ["alg2d", "color"])
 def test_ffr_buf_file_equals_oracle(ffr, fo, tmp_path, name, kernel):
     text = golden_flame_text(name)

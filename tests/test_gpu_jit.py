@@ -1,8 +1,9 @@
 """The per-flame kernels (FFR_KERNEL_JIT) on the GPU, through the C ABI.
 
-A per-flame kernel computes what the general plain kernel computes, with
-each variation slot's type dispatch narrowed at compile time, so for equal
-streams and trajectory lengths its buffers and statistics are the general
+A per-flame kernel computes what the general kernels compute -- the plain
+one with each variation slot's type dispatch narrowed at compile time, the
+xform-sorted one with each xform's types fixed -- so for equal streams and
+trajectory lengths its buffers and statistics are the general plain
 kernel's, bit for bit, in FP64 and FP32: every variation type (the grouped
 flames of jit_cases.py), 1 to 4 dimensions, xforms with and without
 affines, a final xform.  Colour sums are equal to rounding (CTAs add them
@@ -27,7 +28,8 @@ CASES["d4_mixed"] = golden_flame_text("d4_mixed")
 
 @pytest.fixture(scope="module")
 def prepared(ffr):
-    """Compile every case's kernel up front, in parallel."""
+    """Compile every case's kernels (plain and xform-sorted) up front, in
+    parallel."""
     jobs = [(n, p) for n in sorted(CASES) for p in (ffr.FP64, ffr.FP32)]
     with cf.ThreadPoolExecutor(max(2, min(len(jobs), os.cpu_count() or 2))) as ex:
         res = list(ex.map(lambda j: ffr.jit_prepare(CASES[j[0]], j[1]), jobs))
@@ -53,13 +55,19 @@ def same_stats(a, b):
     np.testing.assert_array_equal(a.ext_hi, b.ext_hi)
 
 
+@pytest.mark.parametrize("kernel", [4, 5], ids=["jit", "jit_sorted"])
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_jit_equals_general_kernel(ffr, prepared, name, precision):
+def test_jit_equals_general_kernel(ffr, prepared, name, precision, kernel):
     text = CASES[name]
+    if kernel == ffr.KERNEL_JIT_SORTED and json.loads(text)["dimensions"] > 3:
+        with pytest.raises(ffr.FfrError) as e:
+            render(ffr, text, precision, kernel)
+        assert e.value.status == ffr.FFR_ERR_ARG
+        return
     sp, bp = render(ffr, text, precision, ffr.KERNEL_PLAIN)
-    sj, bj = render(ffr, text, precision, ffr.KERNEL_JIT)
-    assert sp.kernel == ffr.KERNEL_PLAIN and sj.kernel == ffr.KERNEL_JIT
+    sj, bj = render(ffr, text, precision, kernel)
+    assert sp.kernel == ffr.KERNEL_PLAIN and sj.kernel == kernel
     np.testing.assert_array_equal(bj[:, 0], bp[:, 0])
     same_stats(sj, sp)
     assert sj.samples_iterated == 2_000_000
@@ -89,7 +97,8 @@ def test_auto_times_a_prepared_kernel(ffr, flames):
     n = 1 << 25
     sa, ba = render(ffr, text, ffr.FP32, ffr.KERNEL_AUTO, n=n, streams=16384)
     sp, bp = render(ffr, text, ffr.FP32, ffr.KERNEL_PLAIN, n=n, streams=16384)
-    assert sa.kernel in (ffr.KERNEL_PLAIN, ffr.KERNEL_SORTED, ffr.KERNEL_JIT)
+    assert sa.kernel in (ffr.KERNEL_PLAIN, ffr.KERNEL_SORTED, ffr.KERNEL_JIT,
+                         ffr.KERNEL_JIT_SORTED)
     assert sa.aux_launches > 0      # the autotuner's probes
     np.testing.assert_array_equal(ba[:, 0], bp[:, 0])
 

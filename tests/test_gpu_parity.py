@@ -122,9 +122,9 @@ def test_trace_fp32_choices_exact(ffr, name):
 
 # FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED, FFR_KERNEL_HOT (the plain kernel
 # with the flame's hottest cells counted in shared memory)
-# plain, xform-sorted, hot-cell table, per-flame (NVRTC) kernel
-KERNELS = [1, 2, 3, 4]
-KERNEL_IDS = ["plain", "sorted", "hot", "jit"]
+# plain, xform-sorted, hot-cell table, per-flame (NVRTC) plain and sorted
+KERNELS = [1, 2, 3, 4, 5]
+KERNEL_IDS = ["plain", "sorted", "hot", "jit", "jit_sorted"]
 
 
 @pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)

@@ -108,8 +108,8 @@ def test_kernel_option_range(ffr):
     raw = json.dumps({"dimensions": 1, "size": [8], "bounds": [[-1, 1]],
                       "xforms": [{"weight": 1, "variations": [{"name": "linear",
                                                                "weight": 1}]}]}).encode()
-    for kernel, rejected in ((-1, True), (5, True), (ffr.KERNEL_HOT, False),
-                             (ffr.KERNEL_JIT, False)):
+    for kernel, rejected in ((-1, True), (6, True), (ffr.KERNEL_HOT, False),
+                             (ffr.KERNEL_JIT, False), (ffr.KERNEL_JIT_SORTED, False)):
         o = ffr.Opts()
         lib.ffr_default_opts(ctypes.byref(o))
         o.kernel = kernel

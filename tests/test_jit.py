@@ -23,10 +23,14 @@ def test_cases_cover_every_variation():
 
 
 def test_prepare_compiles_every_case(ffr):
-    """Every case in both precisions (NVRTC compiles them in parallel)."""
-    jobs = [(n, p) for n in sorted(CASES) for p in (ffr.FP64, ffr.FP32)]
+    """The plain per-flame kernel of every case in both precisions, and the
+    xform-sorted one of a flame per dimension count (NVRTC compiles them in
+    parallel)."""
+    jobs = [(n, p, ffr.KERNEL_JIT) for n in sorted(CASES) for p in (ffr.FP64, ffr.FP32)]
+    jobs += [(n, ffr.FP64, ffr.KERNEL_JIT_SORTED) for n in ("d1_group0", "d2_group0",
+                                                            "d3_group0")]
     with cf.ThreadPoolExecutor(max(2, min(len(jobs), os.cpu_count() or 2))) as ex:
-        res = list(ex.map(lambda j: ffr.jit_prepare(CASES[j[0]], j[1]), jobs))
+        res = list(ex.map(lambda j: ffr.jit_prepare(CASES[j[0]], j[1], j[2]), jobs))
     bad = [(j, r) for j, r in zip(jobs, res) if r[0] != ffr.FFR_OK]
     assert not bad, bad[:2]
 
@@ -46,7 +50,7 @@ def test_disk_cache_and_merged_programs(ffr, flames, tmp_path, monkeypatch):
     text = json.dumps(flames.random_2d(424242, k=5))
     assert ffr.jit_prepare(text, ffr.FP32)[0] == ffr.FFR_OK
     assert glob.glob(str(tmp_path / "*")) == []
-    st, msg = ffr.jit_prepare(text, ffr.FP64)
+    st, msg = ffr.jit_prepare(text, ffr.FP64, ffr.KERNEL_JIT)
     assert st == ffr.FFR_OK, msg
     keys = glob.glob(str(tmp_path / "ffr_*.key"))
     cubins = glob.glob(str(tmp_path / "ffr_*.cubin"))
@@ -59,8 +63,13 @@ def test_disk_cache_and_merged_programs(ffr, flames, tmp_path, monkeypatch):
     for x in other["xforms"]:
         x["weight"] *= 1.5
         x["pre_affine"]["b"] = [0.25, -0.25]
-    assert ffr.jit_prepare(json.dumps(other), ffr.FP64)[0] == ffr.FFR_OK
+    assert ffr.jit_prepare(json.dumps(other), ffr.FP64, ffr.KERNEL_JIT)[0] == ffr.FFR_OK
     assert len(glob.glob(str(tmp_path / "ffr_*.key"))) == 1
+    # the xform-sorted kernel of the structure: a second entry
+    assert ffr.jit_prepare(text, ffr.FP64, ffr.KERNEL_JIT_SORTED)[0] == ffr.FFR_OK
+    keys = sorted(glob.glob(str(tmp_path / "ffr_*.key")))
+    assert len(keys) == 2
+    assert sum("ffr_flame_sorted(" in open(k).read() for k in keys) == 1
 
 
 def test_prepare_rejects_bad_input(ffr):
