@@ -32,10 +32,11 @@ serving  the Poisson request stream twice: at 200 req/s (over capacity;
         its served rate is the capacity) and at 0.7x that capacity, each
         with p50/p99 latency and its own clock record; latency_ms at the
         top level is the sustainable stream's
-per_flame_kernels  the kernels compiled per flame at run time (NVRTC)
-        against the general plain kernel, same streams, identical buffers:
-        a random 2-D flame of twelve other variations in FP32 and the
-        benchmark flame in the FP64 mirror (3 steps each, with compile time)
+per_flame_kernels  the kernels compiled per flame at run time (NVRTC, plain
+        and xform-sorted) against the general plain and xform-sorted
+        kernels, same streams, identical buffers: a random 2-D flame of
+        twelve other variations in FP32 and FP64, the benchmark flame in the
+        FP64 mirror (3 steps each, with compile time)
 
 tv      FP32 against FP64 at a fixed sample count: total-variation distance
         between the FP32 histogram and an FP64 (reference arithmetic) one,
@@ -476,21 +477,26 @@ NO_BAD_LIMIT = 10**15
 
 
 def per_flame_record(ffr, dev, flames, steps=3):
-    """The per-flame kernels (KERNEL_JIT, NVRTC) against the general plain
-    kernel on flames the precompiled merged instantiations do not cover: a
-    random 2-D flame of parameterless variations outside the benchmark
-    seven (FP32), and the benchmark flame in the FP64 mirror.  Both kernels
-    run the same streams (the plain kernel's default plan), so their
-    buffers must be identical.  No bad-value limit: a render the limit
-    stopped would end early at a time that depends on the race to the stop
-    flag."""
+    """The per-flame kernels (NVRTC: KERNEL_JIT, the plain kernel with each
+    variation slot's dispatch narrowed; KERNEL_JIT_SORTED, the xform-sorted
+    kernel with each xform's types fixed) against the general plain and
+    xform-sorted kernels, on flames the precompiled merged instantiations
+    do not cover: a random 2-D flame of twelve parameterless variations
+    outside the benchmark seven, in FP32 and in the FP64 mirror, and the
+    benchmark flame in the FP64 mirror.  All four kernels run the same
+    streams (the general plain kernel's default plan), so their buffers must
+    be identical.  No bad-value limit: a render the limit stopped would end
+    early at a time that depends on the race to the stop flag."""
     import numpy as np
     import torch
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    other = flames.random_2d(7, variations=flames.OTHER_2D)
     out = []
     for name, fl, prec, n in (
-            ("random 2-D flame of 12 other variations, 1920x1080, FP32",
-             flames.random_2d(7, variations=flames.OTHER_2D), ffr.FP32, 10**9),
+            ("random 2-D flame of 12 other variations, 1920x1080, FP32", other, ffr.FP32,
+             10**9),
+            ("random 2-D flame of 12 other variations, 1920x1080, FP64 mirror", other,
+             ffr.FP64, 10**8),
             ("benchmark flame (6-xform random 1920x1080), FP64 mirror",
              flames.random_2d(7), ffr.FP64, 10**8)):
         text = json.dumps(fl)
@@ -502,8 +508,11 @@ def per_flame_record(ffr, dev, flames, steps=3):
             continue
         rec = {"flame": name, "samples_per_step": n, "compile_s": prep_s}
         plan = None
-        counts = {}
-        for kname, kern in (("general", ffr.KERNEL_PLAIN), ("per_flame", ffr.KERNEL_JIT)):
+        first = None
+        same = True
+        for kname, kern in (("general", ffr.KERNEL_PLAIN), ("general_sorted", ffr.KERNEL_SORTED),
+                            ("per_flame", ffr.KERNEL_JIT),
+                            ("per_flame_sorted", ffr.KERNEL_JIT_SORTED)):
             kw = {} if plan is None else {"streams": plan[0], "traj_len": plan[1]}
             with ffr.BufferRenderer(text, precision=prec, settle=20, device=dev, kernel=kern,
                                     **kw) as r:
@@ -516,16 +525,21 @@ def per_flame_record(ffr, dev, flames, steps=3):
                     flush.zero_()
                     torch.cuda.synchronize()
                     s = r.render(n, 100 + k, bad_limit=NO_BAD_LIMIT)
-                    assert s.ok and s.samples_iterated == n
+                    assert s.ok and s.samples_iterated == n and s.kernel == kern
                     ms += s.kernel_ms
                     binned += s.samples_plotted - s.dropped
                     bad += s.bad_values
                 rec[kname] = {"value": binned / (ms * 1e-3), "unit": "binned samples/s",
-                              "ms_per_step": ms / steps, "kernel": s.kernel,
-                              "bad_values_per_step": bad / steps}
-                counts[kname] = r.counts()
-        rec["speedup"] = rec["general"]["ms_per_step"] / rec["per_flame"]["ms_per_step"]
-        rec["identical_buffers"] = bool(np.array_equal(counts["general"], counts["per_flame"]))
+                              "ms_per_step": ms / steps, "bad_values_per_step": bad / steps}
+                counts = r.counts()
+                if first is None:
+                    first = counts
+                else:
+                    same = same and bool(np.array_equal(first, counts))
+        best_g = min(rec["general"]["ms_per_step"], rec["general_sorted"]["ms_per_step"])
+        best_p = min(rec["per_flame"]["ms_per_step"], rec["per_flame_sorted"]["ms_per_step"])
+        rec["speedup_best_over_best"] = best_g / best_p
+        rec["identical_buffers"] = same
         rec["streams"], rec["traj_len"] = plan
         out.append(rec)
     return out
@@ -540,10 +554,10 @@ def run_perflame(args):
     recs = per_flame_record(ffr, dev, _flames(), steps=max(1, args.steps))
     fp32 = recs[0]["per_flame"]
     _line(args, "per-flame kernels: random 2-D flame of 12 other variations, 1920x1080, "
-          "FP32 (and the benchmark flame, FP64 mirror)", fp32["value"], fp32["ms_per_step"],
+          "FP32 (and FP64 records)", fp32["value"], fp32["ms_per_step"],
           "f32", {"samples_per_step": recs[0]["samples_per_step"], "settle": 20,
                   "flush": "256 MiB L2 flush between timed steps"},
-          gpu_launches=2 * len(recs) * max(1, args.steps), per_flame_kernels=recs)
+          gpu_launches=4 * len(recs) * max(1, args.steps), per_flame_kernels=recs)
 
 
 def run_batch256(args):
