@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -135,6 +136,8 @@ struct ffr_ctx
     // a lower cap runs each thread's streams one after another and never
     // changes which streams run, so the buffer does not depend on it
     int tuned_cap = 0;
+    bool tuned_jit = true;          // TuneChoice::jit_considered, ms_per_sample
+    double tuned_ms_per_sample = 0.0;
     int probe_cap = 0;              // the cap an autotuner probe is planned with
     bool hot_searched = false;      // a hot-cell search ran (probe or autotuner)
     // shape of the last plan(): CTAs per SM allowed, threads per CTA, streams
@@ -350,6 +353,47 @@ ffr_status ensure_jit(ffr_ctx* c, bool sorted, bool ready_only = false)
     if (!k)
         return ready_only ? FFR_ERR_ARG : fail(c, FFR_ERR_CUDA, err);
     return FFR_OK;
+}
+
+// Estimated render time above which the autotuner compiles a flame's
+// per-flame kernels itself: FFR_JIT_AUTO_SECONDS, default 8 (negative: never)
+double jit_auto_seconds()
+{
+    const char* v = std::getenv("FFR_JIT_AUTO_SECONDS");
+    if (!v || !*v)
+        return 8.0;
+    char* end = nullptr;
+    const double s = std::strtod(v, &end);
+    if (end == v)
+        return 8.0;
+    return s < 0 ? 1e300 : s;
+}
+
+// Compile the context's per-flame plain and/or sorted kernels with NVRTC,
+// the two in parallel (failures leave them uncompiled: the autotuner then
+// keeps to the precompiled kernels)
+void compile_jit(ffr_ctx* c, bool plain, bool sorted)
+{
+    const bool color = c->flame.color_dims > 0;
+    if (plain && c->jit_source.empty())
+        c->jit_source = jit_source(c->prog_host, c->opts.precision, color, false);
+    if (sorted && c->jit_sorted_source.empty())
+        c->jit_sorted_source = jit_source(c->prog_host, c->opts.precision, color, true);
+    const int prec = c->opts.precision;
+    auto one = [prec](const std::string* src) {
+        std::string err;
+        if (!src->empty())
+            jit_compile_only(*src, prec, &err);
+    };
+    std::thread t;
+    if (plain && sorted)
+        t = std::thread(one, &c->jit_sorted_source);
+    if (plain)
+        one(&c->jit_source);
+    else if (sorted)
+        one(&c->jit_sorted_source);
+    if (t.joinable())
+        t.join();
 }
 
 // Launch plan: kernel, streams, trajectory length and grid.  The hot-cell
@@ -618,6 +662,11 @@ struct TuneChoice
     int cap = 0;                            // resident CTAs per SM (0: all that fit)
     unsigned int hot_mult = 0;              // 0: no hot-cell table
     std::vector<unsigned int> hot_keys;     // kHotSlots keys when hot_mult != 0
+    // the per-flame kernels were candidates (or do not apply); else the
+    // precompiled candidates' best probe time per sample, by which a longer
+    // render reconsiders them
+    bool jit_considered = true;
+    double ms_per_sample = 0.0;
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneChoice> g_tune_cache;
@@ -743,7 +792,13 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
 {
     const bool spill = c->d_hi != nullptr;
     *hot = false;
-    if (c->tuned && c->tuned_spill == spill)
+    // a decision made without the per-flame kernels stands unless this
+    // render is long enough for them to be compiled
+    auto stands = [&](bool jit_considered, double ms_per_sample) {
+        return jit_considered
+            || ms_per_sample * 1e-3 * (double)samples <= jit_auto_seconds();
+    };
+    if (c->tuned && c->tuned_spill == spill && stands(c->tuned_jit, c->tuned_ms_per_sample))
     {
         *kernel = c->tuned_kernel;
         *agg = c->tuned_agg;
@@ -756,7 +811,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
             auto it = g_tune_cache.find(tune_key(c));
-            if (it != g_tune_cache.end())
+            if (it != g_tune_cache.end()
+                    && stands(it->second.jit_considered, it->second.ms_per_sample))
             {
                 ch = it->second;
                 have = true;
@@ -772,6 +828,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
             c->tuned_kernel = *kernel = ch.kernel;
             c->tuned_agg = *agg = ch.agg;
             c->tuned_cap = ch.cap;
+            c->tuned_jit = ch.jit_considered;
+            c->tuned_ms_per_sample = ch.ms_per_sample;
             c->tuned_hot = *hot = ch.hot_mult != 0;
             c->hot_searched = true;
             return FFR_OK;
@@ -853,19 +911,36 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         }
         return FFR_OK;
     };
-    // the per-flame kernel is a candidate when it is compiled already (an
-    // earlier FFR_KERNEL_JIT render or ffr_jit_prepare, in this process or
-    // in the FFR_JIT_CACHE directory): the autotuner never waits for NVRTC
+    // the per-flame kernels are candidates when compiled already (an
+    // earlier FFR_KERNEL_JIT* render or ffr_jit_prepare, in this process or
+    // in the FFR_JIT_CACHE directory), or when this render would run longer
+    // than jit_auto_seconds() at the best precompiled candidate's probe rate:
+    // the compile (about a second per kernel, the two in parallel) is then
+    // small against the render
     const bool merged = merged_for(c->prog_host.data()) != 0;
-    const bool jit_ready = !merged && ensure_jit(c, false, true) == FFR_OK;
-    const bool jit_sorted_ready = !merged && c->flame.dims <= 3
-        && c->flame.xforms.size() <= (size_t)kSortedMaxXforms
-        && ensure_jit(c, true, true) == FFR_OK;
+    const bool sortable = !merged && c->flame.dims <= 3
+        && c->flame.xforms.size() <= (size_t)kSortedMaxXforms;
+    bool jit_ready = !merged && ensure_jit(c, false, true) == FFR_OK;
+    bool jit_sorted_ready = sortable && ensure_jit(c, true, true) == FFR_OK;
+    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED})
+        for (int g : {0, 1})
+            if (st == FFR_OK)
+                st = probe(k, g, false);
+    const double ms_per_sample = best < 1e30f ? (double)best / (double)P : 0.0;
+    bool jit_considered = merged || (jit_ready && (jit_sorted_ready || !sortable));
+    if (st == FFR_OK && !jit_considered
+            && ms_per_sample * 1e-3 * (double)samples > jit_auto_seconds())
+    {
+        compile_jit(c, !jit_ready, sortable && !jit_sorted_ready);
+        jit_ready = ensure_jit(c, false, true) == FFR_OK;
+        jit_sorted_ready = sortable && ensure_jit(c, true, true) == FFR_OK;
+        jit_considered = true;      // also when NVRTC failed: not retried
+    }
     auto ready = [&](int k) {
         return k == FFR_KERNEL_JIT ? jit_ready : k == FFR_KERNEL_JIT_SORTED ? jit_sorted_ready
                                                                            : true;
     };
-    for (int k : {FFR_KERNEL_PLAIN, FFR_KERNEL_SORTED, FFR_KERNEL_JIT, FFR_KERNEL_JIT_SORTED})
+    for (int k : {FFR_KERNEL_JIT, FFR_KERNEL_JIT_SORTED})
         for (int g : {0, 1})
             if (st == FFR_OK && ready(k))
                 st = probe(k, g, false);
@@ -924,6 +999,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     c->tuned_agg = *agg = best_a;
     c->tuned_hot = *hot = best_h;
     c->tuned_cap = best_cap;
+    c->tuned_jit = jit_considered;
+    c->tuned_ms_per_sample = ms_per_sample;
     // the table (or its absence) is the autotuner's decision: batches reuse it
     c->hot_searched = true;
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -935,6 +1012,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     ch.cap = best_cap;
     ch.hot_mult = mult;
     ch.hot_keys = std::move(keys);
+    ch.jit_considered = jit_considered;
+    ch.ms_per_sample = ms_per_sample;
     g_tune_cache[tune_key(c)] = std::move(ch);
     return FFR_OK;
 }

@@ -118,3 +118,29 @@ def test_jit_default_plan_matches_plain(ffr, flames):
     assert out[0][:2] == out[1][:2]
     assert out[0][2] == out[1][2]
     np.testing.assert_array_equal(out[0][3], out[1][3])
+
+
+@pytest.mark.parametrize("auto_seconds", ["0", "-1"], ids=["compiles", "never"])
+def test_autotuner_compiles_for_long_renders(ffr, flames, tmp_path, monkeypatch, auto_seconds):
+    """A render the autotuner expects to run longer than FFR_JIT_AUTO_SECONDS
+    (0 here: every tuned render) gets its per-flame kernels compiled and
+    timed (both land in the FFR_JIT_CACHE directory); negative: never.
+    Whichever kernel wins, the buffer is the general kernel's."""
+    monkeypatch.setenv("FFR_JIT_CACHE", str(tmp_path))
+    monkeypatch.setenv("FFR_JIT_AUTO_SECONDS", auto_seconds)
+    # a structure no other test compiles (FP64, 5 xforms of other variations)
+    fl = flames.random_2d(34 if auto_seconds == "0" else 35, k=5, size=(480, 270),
+                          variations=["ex", "diamond", "cylinder", "heart", "power", "cosine"])
+    text = json.dumps(fl)
+    n = 1 << 25
+    sa, ba = render(ffr, text, ffr.FP64, ffr.KERNEL_AUTO, n=n, streams=16384)
+    keys = list(tmp_path.glob("ffr_*.key"))
+    if auto_seconds == "0":
+        assert len(keys) == 2
+        assert sa.kernel in (ffr.KERNEL_PLAIN, ffr.KERNEL_SORTED, ffr.KERNEL_JIT,
+                             ffr.KERNEL_JIT_SORTED)
+    else:
+        assert keys == []
+        assert sa.kernel in (ffr.KERNEL_PLAIN, ffr.KERNEL_SORTED)
+    sp, bp = render(ffr, text, ffr.FP64, ffr.KERNEL_PLAIN, n=n, streams=16384)
+    np.testing.assert_array_equal(ba[:, 0], bp[:, 0])
