@@ -102,8 +102,11 @@ typedef struct ffr_opts {
    (stats.kernel PLAIN).  JIT_SORTED: the xform-sorted kernel compiled the
    same way, its warps running each xform's own code (flames of 1..3 dims and
    at most 16 xforms).  AUTO also times the per-flame kernels when they are
-   already compiled.  All choices give identical buffers for equal streams
-   and trajectory lengths. */
+   already compiled, and compiles them itself (about a second each, the two
+   in parallel) when the render would take longer than FFR_JIT_AUTO_SECONDS
+   (environment, default 8; negative: never) with the best precompiled
+   kernel.  All choices give identical buffers for equal streams and
+   trajectory lengths. */
 enum { FFR_KERNEL_AUTO = 0, FFR_KERNEL_PLAIN = 1, FFR_KERNEL_SORTED = 2, FFR_KERNEL_HOT = 3,
        FFR_KERNEL_JIT = 4, FFR_KERNEL_JIT_SORTED = 5 };
 
