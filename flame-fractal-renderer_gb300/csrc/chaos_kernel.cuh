@@ -67,6 +67,21 @@ __device__ __forceinline__ void load_program(unsigned char* dst, const unsigned 
         *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
 }
 
+// 0 + y: the first step of the reference's sums that start from zero
+// (Affine::apply_to's dot products, applyIteration's variation sum), which
+// is y itself except that -0 becomes +0 (and a NaN stays a NaN).  In FP64
+// the sign-bit test and the select run on the integer pipes instead of an
+// FP64 add on the FP64 pipe, which bounds the FP64 kernels on this part; in
+// FP32 the add stays (it is the same fused multiply-add as before).
+template <typename R>
+__device__ __forceinline__ R zero_plus(R y)
+{
+    if constexpr (sizeof(R) == sizeof(double))
+        return __double_as_longlong(y) == (long long)0x8000000000000000ull ? R(0) : y;
+    else
+        return R(0) + y;
+}
+
 // Affine::apply_to: ret = b; ret[i] += (0 + A[i][0] x[0] + ...).  The
 // coefficients (A row-major kMaxDims x kMaxDims, then b; XformT keeps both
 // affines on 16-byte boundaries) come in 16-byte loads, the ones a
@@ -87,9 +102,9 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
 #pragma unroll
     for (int i = 0; i < D; ++i)
     {
-        R d = R(0);
+        R d = zero_plus(c[i * kMaxDims] * x[0]);
 #pragma unroll
-        for (int j = 0; j < D; ++j)
+        for (int j = 1; j < D; ++j)
             d += c[i * kMaxDims + j] * x[j];
         out[i] = c[kMaxDims * kMaxDims + i] + d;
     }
@@ -177,7 +192,14 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
     {
         // every variation of the flame is linear (IFS fractals): v = sum of
         // w_j * t in the reference's accumulation order, no dispatch
-        for (int k = vb; k < ve; ++k)
+        if (vb < ve)
+        {
+            const R w0 = pg.var[vb].weight;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] = zero_plus(t[i] * w0);
+        }
+        for (int k = vb + 1; k < ve; ++k)
         {
             const R w = pg.var[k].weight;
 #pragma unroll
@@ -292,7 +314,7 @@ __device__ __forceinline__ void spec_slots(const Prog<R>& pg, int vb, int n, con
             const R w = var.weight;
 #pragma unroll
             for (int i = 0; i < D; ++i)
-                v[i] += o[i] * w;
+                v[i] = S == 0 ? zero_plus(o[i] * w) : v[i] + o[i] * w;
             spec_slots<SP, S + 1, D, R>(pg, vb, n, t, v, rng, pp);
         }
     }
@@ -319,7 +341,14 @@ __device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT
     if constexpr (SP::present == kTaLinear)
     {
         // every variation of the flame is linear (apply_xform's IFS loop)
-        for (int k = vb; k < vb + n; ++k)
+        if (n > 0)
+        {
+            const R w0 = pg.var[vb].weight;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                v[i] = zero_plus(t[i] * w0);
+        }
+        for (int k = vb + 1; k < vb + n; ++k)
         {
             const R w = pg.var[k].weight;
 #pragma unroll
@@ -363,7 +392,7 @@ __device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT
 // other types share them); PRE / POST: it has the affine (used above 2
 // dims only, as in apply_xform).  The arithmetic is apply_xform's general
 // path on the same program data.
-template <int D, typename R, uint32_t PRESENT, int K, int... TYPES>
+template <int D, typename R, uint32_t PRESENT, bool FIRST, int K, int... TYPES>
 struct FixedVars
 {
     template <typename Rng>
@@ -373,8 +402,8 @@ struct FixedVars
     }
 };
 
-template <int D, typename R, uint32_t PRESENT, int K, int T0, int... REST>
-struct FixedVars<D, R, PRESENT, K, T0, REST...>
+template <int D, typename R, uint32_t PRESENT, bool FIRST, int K, int T0, int... REST>
+struct FixedVars<D, R, PRESENT, FIRST, K, T0, REST...>
 {
     template <typename Rng>
     __device__ static __forceinline__ void run(const Prog<R>& pg, const R* t, R* v, Rng& rng,
@@ -386,8 +415,8 @@ struct FixedVars<D, R, PRESENT, K, T0, REST...>
         const R w = var.weight;
 #pragma unroll
         for (int i = 0; i < D; ++i)
-            v[i] += o[i] * w;
-        FixedVars<D, R, PRESENT, K + 1, REST...>::run(pg, t, v, rng, pp);
+            v[i] = FIRST ? zero_plus(o[i] * w) : v[i] + o[i] * w;
+        FixedVars<D, R, PRESENT, false, K + 1, REST...>::run(pg, t, v, rng, pp);
     }
 };
 
@@ -424,7 +453,7 @@ struct FixedXform
             if (PRESENT & (kTaPolar | kTaJulia))
                 pp.ang = T::atan2_(py, px);
         }
-        FixedVars<D, R, PRESENT, K, TYPES...>::run(pg, t, v, rng, pp);
+        FixedVars<D, R, PRESENT, true, K, TYPES...>::run(pg, t, v, rng, pp);
         if (D < 3 || POST)
             affine<D>(x.post, v, out);
         else
