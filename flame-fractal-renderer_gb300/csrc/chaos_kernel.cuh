@@ -530,13 +530,164 @@ struct RegThresh
 template <int D, typename R>
 __device__ __forceinline__ bool bad_point(const R* p)
 {
-    // |x| > threshold or NaN (utils/flame.hpp:26-29), as one unordered test
+    // |x| > threshold or NaN (utils/flame.hpp:26-29), as one unordered test;
+    // FP64 on the bit patterns (for |x| the IEEE order is the unsigned
+    // order of the bits, and a NaN's bits lie above every finite value's)
     bool b = false;
+    if constexpr (sizeof(R) == sizeof(double))
+    {
+        constexpr unsigned long long kAbs = 0x7fffffffffffffffULL;
+        const unsigned long long thr =
+            (unsigned long long)__double_as_longlong(RealTraits<double>::bad);
 #pragma unroll
-    for (int i = 0; i < D; ++i)
-        b |= !(RealTraits<R>::fabs_(p[i]) <= RealTraits<R>::bad);
+        for (int i = 0; i < D; ++i)
+            b |= ((unsigned long long)__double_as_longlong(p[i]) & kAbs) > thr;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            b |= !(RealTraits<R>::fabs_(p[i]) <= RealTraits<R>::bad);
+    }
     return b;
 }
+
+// the final point inside the bounds: inclusive [lo, hi] per axis
+// (render_iterator.hpp:72-79); NaN is out (documented deviation).  FP64 on
+// ord_key values (launch.h), FP32 as float compares.
+template <int D, typename R>
+__device__ __forceinline__ bool in_bounds(const RenderArgs& a, const R* pf)
+{
+    bool inb = true;
+    if constexpr (sizeof(R) == sizeof(double))
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            const unsigned long long k = ord_key(pf[i]);
+            inb &= (k >= a.lo_key[i]) && (k <= a.hi_key[i]);
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            inb &= (pf[i] >= a.lo_f[i]) && (pf[i] <= a.hi_f[i]);
+    }
+    return inb;
+}
+
+// One thread's running point extremes (buffer_renderer.hpp:188-194: a
+// coordinate below the minimum replaces it, one above the maximum replaces
+// that; a NaN replaces neither), merged over the warp and then into the
+// statistics' order keys.  FP32: min/max instructions.  FP64: ord_key
+// values, min/max on the integer pipes (the order key is the statistics'
+// own encoding; -0 and +0 share a key, within the documented deviation on
+// the sign of a zero extreme).
+template <int D, typename R>
+struct Extremes
+{
+    R lo[D], hi[D];
+    __device__ __forceinline__ void init()
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            lo[i] = R(1) / R(0);
+            hi[i] = -R(1) / R(0);
+        }
+    }
+    __device__ __forceinline__ void update(const R* p)
+    {
+        // one min/max instruction each: the running extreme is never NaN,
+        // and a NaN p keeps it, as the compare does
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            lo[i] = fminf(p[i], lo[i]);
+            hi[i] = fmaxf(p[i], hi[i]);
+        }
+    }
+    __device__ __forceinline__ void warp_reduce()
+    {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+            {
+                const R l = __shfl_down_sync(0xffffffffu, lo[i], off);
+                const R h = __shfl_down_sync(0xffffffffu, hi[i], off);
+                lo[i] = l < lo[i] ? l : lo[i];
+                hi[i] = h > hi[i] ? h : hi[i];
+            }
+    }
+    __device__ __forceinline__ void merge(DevStats* st) const
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            if (lo[i] == lo[i] && lo[i] != R(1) / R(0))
+                atomicMin(&st->ext_lo[i], order_key((double)lo[i]));
+            if (hi[i] == hi[i] && hi[i] != -R(1) / R(0))
+                atomicMax(&st->ext_hi[i], order_key((double)hi[i]));
+        }
+    }
+};
+
+template <int D>
+struct Extremes<D, double>
+{
+    static constexpr unsigned long long kPosInf = 0xfff0000000000000ULL;   // ord_key(+inf)
+    static constexpr unsigned long long kNegInf = 0x000fffffffffffffULL;   // ord_key(-inf)
+    unsigned long long lo[D], hi[D];
+    __device__ __forceinline__ void init()
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            lo[i] = kPosInf;
+            hi[i] = kNegInf;
+        }
+    }
+    __device__ __forceinline__ void update(const double* p)
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            const unsigned long long u = (unsigned long long)__double_as_longlong(p[i]);
+            if ((u & 0x7fffffffffffffffULL) <= 0x7ff0000000000000ULL)   // not NaN
+            {
+                const unsigned long long k = ord_key(p[i]);
+                lo[i] = k < lo[i] ? k : lo[i];
+                hi[i] = k > hi[i] ? k : hi[i];
+            }
+        }
+    }
+    __device__ __forceinline__ void warp_reduce()
+    {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+            {
+                const unsigned long long l = __shfl_down_sync(0xffffffffu, lo[i], off);
+                const unsigned long long h = __shfl_down_sync(0xffffffffu, hi[i], off);
+                lo[i] = l < lo[i] ? l : lo[i];
+                hi[i] = h > hi[i] ? h : hi[i];
+            }
+    }
+    __device__ __forceinline__ void merge(DevStats* st) const
+    {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            if (lo[i] != kPosInf)
+                atomicMin(&st->ext_lo[i], lo[i]);
+            if (hi[i] != kNegInf)
+                atomicMax(&st->ext_hi[i], hi[i]);
+        }
+    }
+};
 
 template <typename R> __device__ __forceinline__ uint64_t to_index(R x);
 template <> __device__ __forceinline__ uint64_t to_index<double>(double x)
@@ -717,13 +868,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
     // below 2^30 cells the index sum (per-axis indices can reach the axis
     // size in FP64, as in the reference) stays under 2^32
     const bool idx32 = a.cells < (1ull << 30);
-    R ext_lo[D], ext_hi[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-    {
-        ext_lo[i] = R(1) / R(0);
-        ext_hi[i] = -R(1) / R(0);
-    }
+    Extremes<D, R> ext;
+    ext.init();
     const int r = COLOR ? a.color_dims : 0;
     R c[COLOR ? kMaxColorDims : 1], cf[COLOR ? kMaxColorDims : 1];
     (void)c; (void)cf;
@@ -850,28 +996,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
                     init();
                 }
                 // extreme coordinates (buffer_renderer.hpp:188-194)
-#pragma unroll
-                for (int i = 0; i < D; ++i)
-                {
-                    if (sizeof(R) == sizeof(float))
-                    {
-                        // one min/max instruction each: the running extreme is
-                        // never NaN, and a NaN p keeps it, as the compare does
-                        ext_lo[i] = fminf(p[i], ext_lo[i]);
-                        ext_hi[i] = fmaxf(p[i], ext_hi[i]);
-                    }
-                    else
-                    {
-                        ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
-                        ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
-                    }
-                }
-                // bounds: inclusive [lo, hi]; NaN is out (documented deviation)
-                bool inb = true;
-#pragma unroll
-                for (int i = 0; i < D; ++i)
-                    inb &= (pf[i] >= G::lo(a, i)) && (pf[i] <= G::hi(a, i));
-                if (inb)
+                ext.update(p);
+                if (in_bounds<D, R>(a, pf))
                 {
                     ++s_plot;
                     uint64_t bi;
@@ -944,15 +1070,8 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
         w_iter += __shfl_down_sync(0xffffffffu, w_iter, off);
         w_plot += __shfl_down_sync(0xffffffffu, w_plot, off);
         w_dropped += __shfl_down_sync(0xffffffffu, w_dropped, off);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-        {
-            const R lo = __shfl_down_sync(0xffffffffu, ext_lo[i], off);
-            const R hi = __shfl_down_sync(0xffffffffu, ext_hi[i], off);
-            ext_lo[i] = lo < ext_lo[i] ? lo : ext_lo[i];
-            ext_hi[i] = hi > ext_hi[i] ? hi : ext_hi[i];
-        }
     }
+    ext.warp_reduce();
     if (lane == 0)
     {
         if (w_iter)
@@ -961,14 +1080,7 @@ __device__ __forceinline__ void chaos_body(const RenderArgs& a, unsigned char* s
             atomicAdd(&a.stats->s_plot, w_plot);
         if (w_dropped)
             atomicAdd(&a.stats->dropped, w_dropped);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-        {
-            if (ext_lo[i] == ext_lo[i] && ext_lo[i] != R(1) / R(0))
-                atomicMin(&a.stats->ext_lo[i], order_key(as_double(ext_lo[i])));
-            if (ext_hi[i] == ext_hi[i] && ext_hi[i] != -R(1) / R(0))
-                atomicMax(&a.stats->ext_hi[i], order_key(as_double(ext_hi[i])));
-        }
+        ext.merge(a.stats);
     }
     if (packed_xfc)
         xflush();

@@ -193,13 +193,8 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
         low = kMaxRefillLow;
 
     unsigned long long s_iter = 0, s_plot = 0, dropped = 0;
-    R ext_lo[D], ext_hi[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-    {
-        ext_lo[i] = R(1) / R(0);
-        ext_hi[i] = -R(1) / R(0);
-    }
+    Extremes<D, R> ext;
+    ext.init();
     const int r = COLOR ? a.color_dims : 0;
     R c[COLOR ? kMaxColorDims : 1], cf[COLOR ? kMaxColorDims : 1];
     (void)c; (void)cf;
@@ -265,17 +260,8 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
     };
     // extremes, bounds, index and binning of a finished sample
     auto tail = [&]() {
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-        {
-            ext_lo[i] = p[i] < ext_lo[i] ? p[i] : ext_lo[i];
-            ext_hi[i] = p[i] > ext_hi[i] ? p[i] : ext_hi[i];
-        }
-        bool inb = true;
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-            inb &= (pf[i] >= h.lo[i]) && (pf[i] <= h.hi[i]);
-        if (!inb)
+        ext.update(p);
+        if (!in_bounds<D, R>(a, pf))
             return;
         ++s_plot;
         uint64_t bi;
@@ -521,15 +507,8 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
         s_iter += __shfl_down_sync(0xffffffffu, s_iter, off);
         s_plot += __shfl_down_sync(0xffffffffu, s_plot, off);
         dropped += __shfl_down_sync(0xffffffffu, dropped, off);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-        {
-            const R lo = __shfl_down_sync(0xffffffffu, ext_lo[i], off);
-            const R hi = __shfl_down_sync(0xffffffffu, ext_hi[i], off);
-            ext_lo[i] = lo < ext_lo[i] ? lo : ext_lo[i];
-            ext_hi[i] = hi > ext_hi[i] ? hi : ext_hi[i];
-        }
     }
+    ext.warp_reduce();
     if (lane == 0)
     {
         if (s_iter)
@@ -538,14 +517,7 @@ __device__ __forceinline__ void sorted_body(const RenderArgs& a, unsigned char* 
             atomicAdd(&a.stats->s_plot, s_plot);
         if (dropped)
             atomicAdd(&a.stats->dropped, dropped);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-        {
-            if (ext_lo[i] == ext_lo[i] && ext_lo[i] != R(1) / R(0))
-                atomicMin(&a.stats->ext_lo[i], order_key(as_double(ext_lo[i])));
-            if (ext_hi[i] == ext_hi[i] && ext_hi[i] != -R(1) / R(0))
-                atomicMax(&a.stats->ext_hi[i], order_key(as_double(ext_hi[i])));
-        }
+        ext.merge(a.stats);
     }
     for (int i = 0; i < nxf; ++i)
     {

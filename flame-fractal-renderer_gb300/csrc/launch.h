@@ -73,7 +73,23 @@ struct RenderArgs
     unsigned int size32[kMaxDims];          // buffer size per axis
     unsigned long long mult_i[kMaxDims];    // cell stride per axis
     unsigned long long cells;
+    // FP64 bounds as ord_key values (the FP64 kernels test bounds on them)
+    unsigned long long lo_key[kMaxDims], hi_key[kMaxDims];
 };
+
+// Monotone 64-bit key of a double with -0 taken as +0: for doubles a, b
+// that are not NaN, a < b exactly when ord_key(a) < ord_key(b), and a == b
+// exactly when the keys are equal.  The FP64 kernels compare and order
+// points on these keys on the integer pipes instead of the FP64 pipe.  A
+// NaN with the sign bit clear keys above +inf, one with it set below -inf.
+__host__ __device__ inline unsigned long long ord_key(double d)
+{
+    unsigned long long u;
+    memcpy(&u, &d, 8);
+    if (u == 0x8000000000000000ULL)
+        u = 0;
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
 
 #ifndef __CUDACC_RTC__
 // copy the geometry of a program blob (precision 0 FP64, 1 FP32) into a
@@ -90,6 +106,8 @@ inline void set_geometry(RenderArgs& a, const void* prog, int precision)
             a.mult_d_d[i] = h.mult_d[i];
             a.size32[i] = (unsigned int)h.size[i];
             a.mult_i[i] = h.mult_i[i];
+            a.lo_key[i] = ord_key(h.lo[i]);
+            a.hi_key[i] = ord_key(h.hi[i]);
         }
         a.cells = h.cells;
     }
