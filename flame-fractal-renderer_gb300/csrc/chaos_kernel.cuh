@@ -110,6 +110,40 @@ __device__ __forceinline__ void affine(const R* aff, const R* x, R* out)
     }
 }
 
+// Affine::apply_to of an absent affine of a 1-D or 2-D xform (the identity,
+// A = I and b = 0, which the reference applies all the same): row i is
+// 0 + ((0 + 1 x_i) + 0 x_j ...), which is x_i with -0 as +0, or NaN when x_i
+// is NaN or another coordinate is infinite or NaN (0 times those is NaN).
+// FP64: the same values from the bit patterns on the integer pipes; FP32:
+// the arithmetic (affine).
+template <int D, typename R>
+__device__ __forceinline__ void identity_affine(const R* aff, const R* x, R* out)
+{
+    if constexpr (sizeof(R) == sizeof(double))
+    {
+        (void)aff;
+        constexpr unsigned long long kAbs = 0x7fffffffffffffffULL;
+        constexpr unsigned long long kInf = 0x7ff0000000000000ULL;
+        bool nonfinite[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+            nonfinite[j] = ((unsigned long long)__double_as_longlong(x[j]) & kAbs) >= kInf;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            const unsigned long long u = (unsigned long long)__double_as_longlong(x[i]);
+            bool nan = (u & kAbs) > kInf;
+#pragma unroll
+            for (int j = 0; j < D; ++j)
+                if (j != i)
+                    nan |= nonfinite[j];
+            out[i] = nan ? __longlong_as_double(0x7fffffffffffffffLL) : zero_plus(x[i]);
+        }
+    }
+    else
+        affine<D>(aff, x, out);
+}
+
 // The merged 2-D application from the compact table (flame_program.h): the
 // same operations in the same order as affine<2> + merged_variations +
 // affine<2> on XformT, from five 16-byte loads instead of eight, so the
@@ -170,8 +204,10 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
             return;
     }
     R t[D], v[D];
-    if (D < 3 || x.has_pre)
+    if (x.has_pre)
         affine<D>(x.pre, p, t);
+    else if (D < 3)
+        identity_affine<D>(x.pre, p, t);
     else
     {
 #pragma unroll
@@ -239,8 +275,10 @@ __device__ __forceinline__ void apply_xform(const Prog<R>& pg, const XformT<R>& 
                 v[i] += o[i] * w;
         }
     }
-    if (D < 3 || x.has_post)
+    if (x.has_post)
         affine<D>(x.post, v, out);
+    else if (D < 3)
+        identity_affine<D>(x.post, v, out);
     else
     {
 #pragma unroll
@@ -326,8 +364,10 @@ __device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT
                                                  const R* p, R* out, Rng& rng)
 {
     R t[D], v[D];
-    if (D < 3 || x.has_pre)
+    if (x.has_pre)
         affine<D>(x.pre, p, t);
+    else if (D < 3)
+        identity_affine<D>(x.pre, p, t);
     else
     {
 #pragma unroll
@@ -374,8 +414,10 @@ __device__ __forceinline__ void apply_xform_spec(const Prog<R>& pg, const XformT
         }
         spec_slots<SP, 0, D, R>(pg, vb, n, t, v, rng, pp);
     }
-    if (D < 3 || x.has_post)
+    if (x.has_post)
         affine<D>(x.post, v, out);
+    else if (D < 3)
+        identity_affine<D>(x.post, v, out);
     else
     {
 #pragma unroll
@@ -428,8 +470,10 @@ struct FixedXform
                                                  const R* p, R* out, Rng& rng)
     {
         R t[D], v[D];
-        if (D < 3 || PRE)
+        if constexpr (PRE)
             affine<D>(x.pre, p, t);
+        else if constexpr (D < 3)
+            identity_affine<D>(x.pre, p, t);
         else
         {
 #pragma unroll
@@ -454,8 +498,10 @@ struct FixedXform
                 pp.ang = T::atan2_(py, px);
         }
         FixedVars<D, R, PRESENT, true, K, TYPES...>::run(pg, t, v, rng, pp);
-        if (D < 3 || POST)
+        if constexpr (POST)
             affine<D>(x.post, v, out);
+        else if constexpr (D < 3)
+            identity_affine<D>(x.post, v, out);
         else
         {
 #pragma unroll
