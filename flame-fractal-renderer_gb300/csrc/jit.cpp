@@ -5,6 +5,7 @@
 #include <dlfcn.h>
 #include <unistd.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -281,12 +282,28 @@ uint64_t fnv1a(const std::string& s)
     return h;
 }
 
+// the kernel headers' text, hashed once: part of every key, so that a
+// library built from other headers never takes a cached cubin of these
+uint64_t headers_hash()
+{
+    static const uint64_t h = [] {
+        std::string all;
+        for (int i = 0; i < kJitHeaderCount; ++i)
+            all += std::string(kJitHeaderNames[i]) + "\n" + kJitHeaderTexts[i];
+        return fnv1a(all);
+    }();
+    return h;
+}
+
+// cache key: compile options, the headers' hash, the source
 std::string key_of(const std::string& src, int precision)
 {
     std::string k;
     for (const std::string& o : options(precision))
         k += o + "\n";
-    return k + src;
+    char hh[40];
+    std::snprintf(hh, sizeof hh, "headers %016llx\n", (unsigned long long)headers_hash());
+    return k + hh + src;
 }
 
 // disk cache (FFR_JIT_CACHE): <hash>.cubin beside <hash>.key holding the
@@ -314,7 +331,9 @@ bool read_file(const std::string& path, std::string* out)
 
 void write_file(const std::string& path, const char* data, size_t n)
 {
-    const std::string tmp = path + ".tmp" + std::to_string((unsigned long)getpid());
+    static std::atomic<unsigned long> serial{0};
+    const std::string tmp = path + ".tmp" + std::to_string((unsigned long)getpid()) + "."
+        + std::to_string(serial++);
     {
         std::ofstream f(tmp, std::ios::binary);
         if (!f)

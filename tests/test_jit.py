@@ -7,6 +7,7 @@ import concurrent.futures as cf
 import glob
 import json
 import os
+import re
 
 import jit_cases
 from conftest import golden_flame_text
@@ -56,7 +57,10 @@ def test_disk_cache_and_merged_programs(ffr, flames, tmp_path, monkeypatch):
     cubins = glob.glob(str(tmp_path / "ffr_*.cubin"))
     assert len(keys) == 1 and len(cubins) == 1
     key = open(keys[0]).read()
+    # the options, a hash of the kernel headers the library embeds (a rebuilt
+    # library never takes another build's cubin) and the source
     assert "--fmad=false" in key and "struct FlameSpec" in key
+    assert re.search(r"^headers [0-9a-f]{16}$", key, re.M)
     assert os.path.getsize(cubins[0]) > 1000
     # same structure, other weights and affines: the same kernel
     other = json.loads(text)
