@@ -28,10 +28,11 @@ cpu_baseline  the oracle's C restatement of the reference path (FP64,
         (port_vs_reference, oracle/port_vs_reference.py)
 batch256  the 256-flame batch in one persistent graph launch (2 timed
         steps, per-flame TV of 8 flames against FP64)
-serving  the Poisson request stream twice: at 200 req/s (over capacity;
-        its served rate is the capacity) and at 0.7x that capacity, each
-        with p50/p99 latency and its own clock record; latency_ms at the
-        top level is the sustainable stream's
+serving  the Poisson request stream three times, each with p50/p99 latency
+        and its own clock record: the configured 200 req/s, the same stream
+        at 400 req/s (saturated: its served samples/s is the capacity), and
+        0.7x that capacity; latency_ms at the top level is the configured
+        stream's, with the sustainable one's beside it
 per_flame_kernels  the kernels compiled per flame at run time (NVRTC, plain
         and xform-sorted) against the general plain and xform-sorted
         kernels, same streams, identical buffers: a random 2-D flame of
@@ -937,20 +938,28 @@ def main():
     if ws == 1 and not args.no_sub:
         per_flame = per_flame_record(ffr, local, flames)
         batch = batch256_record(ffr, local, steps=2, warmup=1, with_tv=not args.no_tv)
-        over = serving_record(ffr, local, 200.0, args.serving_seconds, 1, args.max_active,
+        # the configured stream (200 req/s); the same stream at twice the
+        # rate, whose served samples/s is the loop's capacity when the loop
+        # falls behind it (served below 95% of offered); then 0.7 x capacity
+        conf = serving_record(ffr, local, 200.0, args.serving_seconds, 1, args.max_active,
                               with_tv=False)
-        per_req = over["offered_samples_per_s"] / over["rate_per_s"]
-        capacity = over["iterated_per_s"] / per_req
+        sat = serving_record(ffr, local, 400.0, max(4.0, args.serving_seconds / 2), 1,
+                             args.max_active, with_tv=False)
+        per_req = conf["offered_samples_per_s"] / conf["rate_per_s"]
+        saturated = sat["iterated_per_s"] < 0.95 * sat["offered_samples_per_s"]
+        capacity = max(conf["iterated_per_s"], sat["iterated_per_s"]) / per_req
         rate = round(0.7 * capacity, 1)
         steady = serving_record(ffr, local, rate, args.serving_seconds * 1.5, 1,
                                 args.max_active, with_tv=not args.no_tv)
         serving = {
+            "configured": dict(conf, what="the configured stream, 200 req/s"),
+            "saturated": dict(sat, what="400 req/s: when the loop falls behind, its served "
+                              "samples/s is the capacity and latency measures queue growth"),
             "sustainable": dict(steady, what=f"0.7 x the measured capacity "
-                                f"({capacity:.1f} req/s = {over['iterated_per_s']:.3g} "
-                                f"samples/s / {per_req:.3g} samples per request)"),
-            "over_capacity": dict(over, what="200 req/s: offered samples/s above capacity, "
-                                  "so latency measures queue growth, not service time"),
+                                f"({capacity:.1f} req/s = served samples/s / {per_req:.3g} "
+                                f"samples per request)"),
             "capacity_req_per_s": capacity,
+            "capacity_is_lower_bound": not saturated,
         }
 
     line = {
@@ -982,9 +991,15 @@ def main():
         "per_flame_kernels": per_flame,
     }
     if serving:
-        line["latency_ms"] = {"p50": serving["sustainable"]["latency_ms"]["p50"],
-                              "p99": serving["sustainable"]["latency_ms"]["p99"],
-                              "rate_per_s": serving["sustainable"]["rate_per_s"]}
+        # the configured stream's latency (the loop keeps up with it), and
+        # the sustainable stream's
+        line["latency_ms"] = {"p50": serving["configured"]["latency_ms"]["p50"],
+                              "p99": serving["configured"]["latency_ms"]["p99"],
+                              "rate_per_s": serving["configured"]["rate_per_s"],
+                              "sustainable": {
+                                  "p50": serving["sustainable"]["latency_ms"]["p50"],
+                                  "p99": serving["sustainable"]["latency_ms"]["p99"],
+                                  "rate_per_s": serving["sustainable"]["rate_per_s"]}}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
