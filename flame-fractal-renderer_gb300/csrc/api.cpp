@@ -875,12 +875,42 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         if (e != cudaSuccess)
             st = cuda_fail(c, e, "autotune scratch");
     }
+    // The probes run as many streams at once as the render will (with
+    // proportionally shorter trajectories), whatever streams and trajectory
+    // length the context fixes: contention on hot cells, which decides
+    // between the candidates, grows with the threads binning at once, and a
+    // probe of P samples in the context's own long trajectories could run on
+    // a few thousand threads.  The probes render into scratch buffers, so
+    // their streams never reach the context's buffer.
+    uint64_t probe_streams = 0, probe_len = 0;
+    {
+        uint64_t S0 = 0, L0 = 0;
+        int g0 = 0, k0 = 0;
+        if (plan(c, samples, FFR_KERNEL_PLAIN, &S0, &L0, &g0, &k0) == FFR_OK && L0 > 0)
+        {
+            const uint64_t ntraj = (samples + L0 - 1) / L0;
+            probe_streams = std::max<uint64_t>(1, std::min<uint64_t>(S0, ntraj));
+            probe_len = std::max<uint64_t>(1, P / probe_streams);
+        }
+    }
     // one candidate: time two probe launches, keep the faster candidate
     auto probe = [&](int k, int g, bool h) -> ffr_status {
         uint64_t S = 0, L = 0;
         int grid = 0, kk = 0;
         bool hh = h;
-        if (plan(c, P, k, &S, &L, &grid, &kk, &hh) != FFR_OK || hh != h)
+        ffr_status ps;
+        {
+            const uint64_t saved_s = c->opts.streams, saved_l = c->opts.traj_len;
+            if (probe_streams)
+            {
+                c->opts.streams = probe_streams;
+                c->opts.traj_len = probe_len;
+            }
+            ps = plan(c, P, k, &S, &L, &grid, &kk, &hh);
+            c->opts.streams = saved_s;
+            c->opts.traj_len = saved_l;
+        }
+        if (ps != FFR_OK || hh != h)
             return FFR_OK;      // candidate does not apply to this flame
         RenderArgs a;
         fill_args(c, a, P, 0x5eedull + (uint64_t)k * 2 + g, ~0ull, S, L, pc, ph, pcol, pst, g);
