@@ -1995,8 +1995,16 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
                                        sizeof(JobDesc) * g.members.size() + sizeof(BatchHead),
                                        cudaMemcpyHostToDevice, b->stream));
             }
+            // the members' buffers (counts, high words, colour sums)
+            std::vector<unsigned long long> bytes(g.members.size());
+            for (size_t k = 0; k < g.members.size(); ++k)
+            {
+                const ffr_ctx* m = b->ctxs[g.members[k]];
+                bytes[k] = (unsigned long long)m->flame.cells
+                    * (4ull + (m->d_hi ? 4ull : 0ull) + 8ull * (unsigned long long)m->flame.color_dims);
+            }
             std::vector<unsigned long long> order;
-            interleave_chunks(counts, order);
+            interleave_chunks(counts, order, &bytes);
             std::memcpy(g.h_order, order.data(), order.size() * sizeof(unsigned long long));
             BCU(b, cudaMemcpyAsync(g.d_order, g.h_order, order.size() * sizeof(unsigned long long),
                                    cudaMemcpyHostToDevice, b->stream));

@@ -303,9 +303,18 @@ struct BatchArgs
 // so every job advances at the same relative pace and concurrent CTAs spread
 // over the jobs in proportion to their size.  (Binning every CTA into one
 // job's buffer at a time concentrates the L2 atomics: the 256-flame batch
-// ran 27% slower in job order.)  Any order gives the same buffers.
+// ran 27% slower in job order.)  With bytes (each job's buffer size), the
+// jobs are taken in windows of consecutive jobs -- at least kMinWindowJobs,
+// and more while their buffers add up to at most kWindowBytes -- interleaved
+// within a window, one window after another, so that the buffers the running
+// CTAs bin into stay within L2 instead of every buffer of a large batch
+// being in flight at once.  Any order gives the same buffers.
+constexpr size_t kMinWindowJobs = 16;
+constexpr unsigned long long kWindowBytes = 64ull << 20;
+
 inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
-                              std::vector<unsigned long long>& order)
+                              std::vector<unsigned long long>& order,
+                              const std::vector<unsigned long long>* bytes = nullptr)
 {
     order.clear();
     struct Item
@@ -317,20 +326,34 @@ inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
             return key > o.key || (key == o.key && job > o.job);
         }
     };
-    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
-    for (size_t k = 0; k < chunks.size(); ++k)
-        if (chunks[k])
-            heap.push({0.5 / (double)chunks[k], k, 0});
-    while (!heap.empty())
+    size_t k0 = 0;
+    while (k0 < chunks.size())
     {
-        Item it = heap.top();
-        heap.pop();
-        order.push_back((it.job << 32) | it.r);
-        if (++it.r < chunks[it.job])
+        size_t k1 = chunks.size();
+        if (bytes)
         {
-            it.key = ((double)it.r + 0.5) / (double)chunks[it.job];
-            heap.push(it);
+            unsigned long long sum = 0;
+            k1 = k0;
+            while (k1 < chunks.size()
+                   && (k1 - k0 < kMinWindowJobs || sum + (*bytes)[k1] <= kWindowBytes))
+                sum += (*bytes)[k1++];
         }
+        std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+        for (size_t k = k0; k < k1; ++k)
+            if (chunks[k])
+                heap.push({0.5 / (double)chunks[k], k, 0});
+        while (!heap.empty())
+        {
+            Item it = heap.top();
+            heap.pop();
+            order.push_back((it.job << 32) | it.r);
+            if (++it.r < chunks[it.job])
+            {
+                it.key = ((double)it.r + 0.5) / (double)chunks[it.job];
+                heap.push(it);
+            }
+        }
+        k0 = k1;
     }
 }
 #endif

@@ -373,6 +373,10 @@ void Server::admit_locked()
     }
 }
 
+// jobs with at most this many chunks (128 streams each) left join every
+// round (they finish in it)
+constexpr uint64_t kSmallJobChunks = 32;
+
 // Build and launch one round on a free round slot; false if there is no
 // free slot or no chunk left to issue.
 bool Server::launch_round_locked()
@@ -386,10 +390,33 @@ bool Server::launch_round_locked()
     }
     if (!r || broken)
         return false;
+    // The round's jobs: the oldest ones while their buffers add up to at
+    // most kWindowBytes (at least kMinWindowJobs of them, launch.h), so that
+    // the buffers a round bins into stay within L2, plus every job that this
+    // round can finish outright (at most kSmallJobChunks chunks left), so
+    // that small jobs never wait behind large ones.  (Rounds over every
+    // running job kept hundreds of buffers, gigabytes, in flight at once.)
     std::vector<SrvJob*> cand;
-    for (SrvJob* j : active)
-        if (!j->cancel_req && j->chunks_issued < j->chunks_total)
-            cand.push_back(j);
+    {
+        size_t in_window = 0;
+        unsigned long long window_bytes = 0;
+        for (SrvJob* j : active)
+        {
+            if (j->cancel_req || j->chunks_issued >= j->chunks_total)
+                continue;
+            const SrvBuffer& b = *j->buf;
+            const unsigned long long bytes = (unsigned long long)b.flame.cells
+                * (4ull + 8ull * (unsigned long long)b.flame.color_dims);
+            if (in_window < kMinWindowJobs || window_bytes + bytes <= kWindowBytes)
+            {
+                ++in_window;
+                window_bytes += bytes;
+                cand.push_back(j);
+            }
+            else if (j->chunks_total - j->chunks_issued <= kSmallJobChunks)
+                cand.push_back(j);
+        }
+    }
     if (cand.empty())
         return false;
     uint64_t budget_chunks = o.round_chunks;
@@ -400,7 +427,7 @@ bool Server::launch_round_locked()
         launchers(o.precision, b0.flame.dims).occ_batch(b0.flame.color_dims > 0,
                                                         merged_for(b0.prog.data()), &bps,
                                                         &block, b0.smem);
-        budget_chunks = 2ull * (uint64_t)sms * (uint64_t)std::max(1, bps);
+        budget_chunks = 4ull * (uint64_t)sms * (uint64_t)std::max(1, bps);
     }
     budget_chunks = std::min<uint64_t>(budget_chunks, r->order_cap);
     // even share, then what is left to the oldest jobs

@@ -315,7 +315,7 @@ typedef struct ffr_server_opts {
        0 = free device memory at creation minus 2 GiB */
     uint64_t hbm_budget;
     uint64_t max_active;       /* jobs admitted at once; default 256 */
-    uint64_t round_chunks;     /* chunks per round; 0 = twice the resident CTAs */
+    uint64_t round_chunks;     /* chunks per round; 0 = four times the resident CTAs */
     uint64_t timeout_ms;       /* limit of one round's device work; 0 = none */
 } ffr_server_opts;
 
