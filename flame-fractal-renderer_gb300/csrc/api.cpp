@@ -2004,7 +2004,7 @@ ffr_status ffr_batch_render(ffr_batch* b, const uint64_t* samples, const uint64_
                     * (4ull + (m->d_hi ? 4ull : 0ull) + 8ull * (unsigned long long)m->flame.color_dims);
             }
             std::vector<unsigned long long> order;
-            interleave_chunks(counts, order, &bytes);
+            interleave_chunks(counts, order, &bytes, 2ull * (unsigned long long)g.grid);
             std::memcpy(g.h_order, order.data(), order.size() * sizeof(unsigned long long));
             BCU(b, cudaMemcpyAsync(g.d_order, g.h_order, order.size() * sizeof(unsigned long long),
                                    cudaMemcpyHostToDevice, b->stream));

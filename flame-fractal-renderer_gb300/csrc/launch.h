@@ -304,8 +304,9 @@ struct BatchArgs
 // over the jobs in proportion to their size.  (Binning every CTA into one
 // job's buffer at a time concentrates the L2 atomics: the 256-flame batch
 // ran 27% slower in job order.)  With bytes (each job's buffer size), the
-// jobs are taken in windows of consecutive jobs -- at least kMinWindowJobs,
-// and more while their buffers add up to at most kWindowBytes -- interleaved
+// jobs are taken in windows of consecutive jobs -- at least kMinWindowJobs
+// jobs and min_chunks chunks (enough to keep every resident CTA busy), and
+// more while their buffers add up to at most kWindowBytes -- interleaved
 // within a window, one window after another, so that the buffers the running
 // CTAs bin into stay within L2 instead of every buffer of a large batch
 // being in flight at once.  Any order gives the same buffers.
@@ -314,7 +315,8 @@ constexpr unsigned long long kWindowBytes = 64ull << 20;
 
 inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
                               std::vector<unsigned long long>& order,
-                              const std::vector<unsigned long long>* bytes = nullptr)
+                              const std::vector<unsigned long long>* bytes = nullptr,
+                              unsigned long long min_chunks = 0)
 {
     order.clear();
     struct Item
@@ -332,11 +334,15 @@ inline void interleave_chunks(const std::vector<unsigned long long>& chunks,
         size_t k1 = chunks.size();
         if (bytes)
         {
-            unsigned long long sum = 0;
+            unsigned long long sum = 0, n = 0;
             k1 = k0;
             while (k1 < chunks.size()
-                   && (k1 - k0 < kMinWindowJobs || sum + (*bytes)[k1] <= kWindowBytes))
-                sum += (*bytes)[k1++];
+                   && (k1 - k0 < kMinWindowJobs || n < min_chunks
+                       || sum + (*bytes)[k1] <= kWindowBytes))
+            {
+                sum += (*bytes)[k1];
+                n += chunks[k1++];
+            }
         }
         std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
         for (size_t k = k0; k < k1; ++k)
