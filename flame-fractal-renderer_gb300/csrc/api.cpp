@@ -236,20 +236,107 @@ ffr_status wait_stream(ffr_ctx* c)
         + std::to_string(limit) + " ms) and was cancelled");
 }
 
+// Context buffers come from a per-device stream-ordered pool that keeps up
+// to kPoolKeepBytes of the memory of destroyed contexts for the next ones
+// (allocated and freed in order on the context's stream): creating and
+// destroying a context per render, as a caller of ffr_create / ffr_render /
+// ffr_destroy does, then costs no device-wide synchronisation and no driver
+// allocation, while memory beyond that returns to the device.
+constexpr unsigned long long kPoolKeepBytes = 4ull << 30;
+std::mutex g_pool_mu;
+std::map<int, cudaMemPool_t> g_pools;
+
+cudaError_t ctx_pool(int device, cudaMemPool_t* out)
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pools.find(device);
+    if (it != g_pools.end())
+    {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof props);
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess)
+        return e;
+    unsigned long long keep = kPoolKeepBytes;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess)
+    {
+        cudaMemPoolDestroy(pool);
+        return e;
+    }
+    g_pools[device] = pool;
+    *out = pool;
+    return cudaSuccess;
+}
+
+// bytes the device's context pool holds without an allocation using them
+// (free for a new context, although cudaMemGetInfo counts them as used)
+size_t pool_cached(int device)
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pools.find(device);
+    if (it == g_pools.end())
+        return 0;
+    unsigned long long reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(it->second, cudaMemPoolAttrReservedMemCurrent, &reserved)
+            != cudaSuccess
+        || cudaMemPoolGetAttribute(it->second, cudaMemPoolAttrUsedMemCurrent, &used)
+            != cudaSuccess)
+        return 0;
+    return reserved > used ? (size_t)(reserved - used) : 0;
+}
+
+// free device memory for a context: the device's free memory plus its
+// context pool's unused bytes
+cudaError_t ctx_free_bytes(int device, size_t* fr)
+{
+    size_t tot = 0;
+    cudaError_t e = cudaMemGetInfo(fr, &tot);
+    if (e == cudaSuccess)
+        *fr += pool_cached(device);
+    return e;
+}
+
+template <typename T>
+cudaError_t ctx_alloc(ffr_ctx* c, T** p, size_t bytes)
+{
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = ctx_pool(c->device, &pool);
+    if (e != cudaSuccess)
+        return e;
+    void* v = nullptr;
+    e = cudaMallocFromPoolAsync(&v, bytes, pool, c->stream);
+    *p = static_cast<T*>(v);
+    return e;
+}
+
+void ctx_release(ffr_ctx* c, void* p)
+{
+    if (p)
+        cudaFreeAsync(p, c->stream);
+}
+
 ffr_status ensure_scratch(ffr_ctx* c, size_t bytes)
 {
     if (c->scratch_bytes >= bytes)
         return FFR_OK;
-    if (c->d_scratch)
-        cudaFree(c->d_scratch);
+    ctx_release(c, c->d_scratch);
     c->d_scratch = nullptr;
     c->scratch_bytes = 0;
-    size_t fr = 0, tot = 0;
-    CU(c, cudaMemGetInfo(&fr, &tot));
+    size_t fr = 0;
+    CU(c, ctx_free_bytes(c->device, &fr));
     if (bytes + (64u << 20) > fr)
         return fail(c, FFR_ERR_OOM, "not enough free device memory for a "
             + std::to_string(bytes) + "-byte staging buffer");
-    CU(c, cudaMalloc(&c->d_scratch, bytes));
+    CU(c, ctx_alloc(c, &c->d_scratch, bytes));
     c->scratch_bytes = bytes;
     return FFR_OK;
 }
@@ -258,7 +345,7 @@ ffr_status ensure_hi(ffr_ctx* c)
 {
     if (c->d_hi)
         return FFR_OK;
-    CU(c, cudaMalloc(&c->d_hi, c->flame.cells * sizeof(unsigned int)));
+    CU(c, ctx_alloc(c, &c->d_hi, c->flame.cells * sizeof(unsigned int)));
     CU(c, cudaMemsetAsync(c->d_hi, 0, c->flame.cells * sizeof(unsigned int), c->stream));
     return FFR_OK;
 }
@@ -309,14 +396,17 @@ void destroy(ffr_ctx* c)
         return;
     cudaSetDevice(c->device);
     if (c->stream)
+    {
+        // back to the pool in stream order, then wait for the stream
+        ctx_release(c, c->d_prog);
+        ctx_release(c, c->d_counts);
+        ctx_release(c, c->d_hi);
+        ctx_release(c, c->d_colors);
+        ctx_release(c, c->d_stats);
+        ctx_release(c, c->d_scratch);
+        ctx_release(c, c->d_hot);
         cudaStreamSynchronize(c->stream);
-    cudaFree(c->d_prog);
-    cudaFree(c->d_counts);
-    cudaFree(c->d_hi);
-    cudaFree(c->d_colors);
-    cudaFree(c->d_stats);
-    cudaFree(c->d_scratch);
-    cudaFree(c->d_hot);
+    }
     if (c->h_cancel)
         give_flag(c->device, c->h_cancel, c->d_cancel);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -713,7 +803,7 @@ ffr_status set_hot(ffr_ctx* c, unsigned int mult, const std::vector<unsigned int
     if (mult == 0)
         return FFR_OK;
     if (!c->d_hot)
-        CU(c, cudaMalloc(&c->d_hot, kHotSlots * sizeof(unsigned int)));
+        CU(c, ctx_alloc(c, &c->d_hot, kHotSlots * sizeof(unsigned int)));
     CU(c, cudaMemcpyAsync(c->d_hot, keys.data(), kHotSlots * sizeof(unsigned int),
                           cudaMemcpyHostToDevice, c->stream));
     CU(c, cudaStreamSynchronize(c->stream));
@@ -1132,8 +1222,8 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
     const size_t need = c->flame.cells * sizeof(unsigned int)
         + c->flame.cells * (size_t)c->flame.color_dims * sizeof(double)
         + sizeof(DevStats) + c->prog_host.size();
-    size_t fr = 0, tot = 0;
-    if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess)
+    size_t fr = 0;
+    if ((e = ctx_free_bytes(c->device, &fr)) != cudaSuccess)
         return cfail(e, "cudaMemGetInfo");
     if (need + (256u << 20) > fr)
     {
@@ -1141,14 +1231,15 @@ ffr_status ffr_create(const char* json, size_t len, const ffr_opts* opts, ffr_ct
         return fail(nullptr, FFR_ERR_OOM, "buffer needs " + std::to_string(need)
             + " bytes of device memory, " + std::to_string(fr) + " free");
     }
-    if ((e = cudaMalloc(&c->d_prog, c->prog_host.size())) != cudaSuccess)
+    if ((e = ctx_alloc(c, &c->d_prog, c->prog_host.size())) != cudaSuccess)
         return cfail(e, "cudaMalloc(program)");
-    if ((e = cudaMalloc(&c->d_counts, c->flame.cells * sizeof(unsigned int))) != cudaSuccess)
+    if ((e = ctx_alloc(c, &c->d_counts, c->flame.cells * sizeof(unsigned int))) != cudaSuccess)
         return cfail(e, "cudaMalloc(counts)");
     if (c->flame.color_dims
-            && (e = cudaMalloc(&c->d_colors, c->flame.cells * c->flame.color_dims * sizeof(double))) != cudaSuccess)
+            && (e = ctx_alloc(c, &c->d_colors,
+                              c->flame.cells * c->flame.color_dims * sizeof(double))) != cudaSuccess)
         return cfail(e, "cudaMalloc(colors)");
-    if ((e = cudaMalloc(&c->d_stats, sizeof(DevStats))) != cudaSuccess)
+    if ((e = ctx_alloc(c, &c->d_stats, sizeof(DevStats))) != cudaSuccess)
         return cfail(e, "cudaMalloc(stats)");
     if ((e = cudaMemcpyAsync(c->d_prog, c->prog_host.data(), c->prog_host.size(),
                              cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
