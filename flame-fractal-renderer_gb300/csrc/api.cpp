@@ -341,12 +341,16 @@ ffr_status ensure_scratch(ffr_ctx* c, size_t bytes)
     return FFR_OK;
 }
 
+// The high-word buffer, zeroed; the wait makes it ready for any stream (a
+// batch renders on its own stream; pool memory and the memset are ordered
+// on the context's)
 ffr_status ensure_hi(ffr_ctx* c)
 {
     if (c->d_hi)
         return FFR_OK;
     CU(c, ctx_alloc(c, &c->d_hi, c->flame.cells * sizeof(unsigned int)));
     CU(c, cudaMemsetAsync(c->d_hi, 0, c->flame.cells * sizeof(unsigned int), c->stream));
+    CU(c, cudaStreamSynchronize(c->stream));
     return FFR_OK;
 }
 
