@@ -1,102 +1,87 @@
-"""Host logic of the batch claim order (interleave_chunks, launch.h), compiled
-with the host compiler: every (job, chunk) pair exactly once, chunks of a job
-in order, jobs interleaved by relative pace, and with buffer sizes the
-windows of consecutive jobs (at least kMinWindowJobs jobs and min_chunks
-chunks, more while the buffers fit kWindowBytes)."""
-import json
+"""Claim order of the persistent batch kernel (interleave_chunks, launch.h;
+host-only, no GPU): chunk r of job k sits at key (r + 1/2) / chunks_k, so
+every job advances at the same relative pace.  A small driver compiled
+against the header prints the order for given chunk counts."""
+import importlib.util
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
 
-CSRC = os.path.join(ROOT, "flame-fractal-renderer_gb300", "csrc")
+PKG = os.path.join(ROOT, "flame-fractal-renderer_gb300")
 
 DRIVER = r"""
+#include "launch.h"
 #include <cstdio>
 #include <vector>
-#include "launch.h"
-using namespace ffr;
 int main()
 {
-    // jobs: chunk counts and buffer bytes (MB)
-    unsigned long long chunks_in[] = {@CHUNKS@};
-    unsigned long long mb_in[] = {@MBS@};
-    const size_t n = sizeof chunks_in / sizeof chunks_in[0];
-    std::vector<unsigned long long> chunks(chunks_in, chunks_in + n), bytes(n);
-    for (size_t k = 0; k < n; ++k)
-        bytes[k] = mb_in[k] << 20;
-    std::vector<unsigned long long> order;
-    interleave_chunks(chunks, order, @WITH_BYTES@ ? &bytes : nullptr, @MIN_CHUNKS@);
-    std::printf("{\"min_jobs\": %zu, \"window_mb\": %llu, \"order\": [", kMinWindowJobs,
-                kWindowBytes >> 20);
-    for (size_t i = 0; i < order.size(); ++i)
-        std::printf("%s[%llu, %llu]", i ? ", " : "", order[i] >> 32, order[i] & 0xffffffffull);
-    std::printf("]}\n");
+    unsigned long long n = 0;
+    while (std::scanf("%llu", &n) == 1)
+    {
+        std::vector<unsigned long long> chunks(n), order;
+        for (auto& c : chunks)
+            if (std::scanf("%llu", &c) != 1)
+                return 1;
+        ffr::interleave_chunks(chunks, order);
+        std::printf("%zu", order.size());
+        for (unsigned long long e : order)
+            std::printf(" %llu", e);
+        std::printf("\n");
+    }
     return 0;
 }
 """
 
 
-def cuda_include():
-    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
-        if c and os.path.exists(os.path.join(c, "include", "cuda_runtime.h")):
-            return os.path.join(c, "include")
-    pytest.skip("CUDA headers not found")
+@pytest.fixture(scope="module")
+def order_of(tmp_path_factory):
+    spec = importlib.util.spec_from_file_location("ffr_build", os.path.join(PKG, "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    d = tmp_path_factory.mktemp("order")
+    src = d / "driver.cpp"
+    src.write_text(DRIVER)
+    exe = d / "driver"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(PKG, "csrc"),
+                           "-I", os.path.join(ROOT, "include"),
+                           "-I", os.path.join(b._cuda_home(), "include"), str(src),
+                           "-o", str(exe)])
+
+    def run(chunks):
+        text = f"{len(chunks)} " + " ".join(str(c) for c in chunks) + "\n"
+        out = subprocess.run([str(exe)], input=text, capture_output=True, text=True,
+                             check=True).stdout.split()
+        n = int(out[0])
+        return [(int(e) >> 32, int(e) & 0xFFFFFFFF) for e in out[1:1 + n]]
+    return run
 
 
-def run_order(tmp_path, chunks, mbs, with_bytes, min_chunks=0):
-    src = (DRIVER.replace("@CHUNKS@", ", ".join(map(str, chunks)))
-           .replace("@MBS@", ", ".join(map(str, mbs)))
-           .replace("@WITH_BYTES@", "1" if with_bytes else "0")
-           .replace("@MIN_CHUNKS@", str(min_chunks)))
-    c = tmp_path / "order.cpp"
-    c.write_text(src)
-    exe = tmp_path / "order"
-    subprocess.check_call(["g++", "-std=c++17", "-O1", "-I", CSRC, "-I", cuda_include(),
-                           str(c), "-o", str(exe)])
-    return json.loads(subprocess.check_output([str(exe)], text=True))
+@pytest.mark.parametrize("chunks", [[1], [5, 0, 3], [7, 7, 7], [1, 1000, 13, 0, 250],
+                                    list(range(1, 40))])
+def test_every_chunk_once_in_job_order(order_of, chunks):
+    order = order_of(chunks)
+    assert sorted(order) == sorted((k, r) for k, c in enumerate(chunks) for r in range(c))
+    last = {}
+    for k, r in order:
+        assert r == last.get(k, -1) + 1        # a job's chunks in ascending order
+        last[k] = r
 
 
-def check_permutation(order, chunks):
-    seen = {}
-    for job, r in order:
-        assert r == seen.get(job, 0), "chunks of a job in order"
-        seen[job] = r + 1
-    assert seen == {k: c for k, c in enumerate(chunks) if c}
+def test_jobs_advance_at_the_same_relative_pace(order_of):
+    g = np.random.Generator(np.random.PCG64(3))
+    chunks = g.integers(1, 500, size=64).tolist()
+    order = order_of(chunks)
+    keys = [(r + 0.5) / chunks[k] for k, r in order]
+    assert all(a <= b for a, b in zip(keys, keys[1:]))
+    # halfway through the order every job is about halfway through its chunks
+    half = order[:len(order) // 2]
+    done = np.bincount([k for k, _ in half], minlength=len(chunks))
+    assert np.all(np.abs(done / np.array(chunks) - 0.5) <= 1.0 / np.array(chunks) + 1e-9)
 
 
-def test_interleaved_without_sizes(tmp_path):
-    chunks = [4, 1, 8, 0, 2]
-    out = run_order(tmp_path, chunks, [1] * len(chunks), False)
-    order = out["order"]
-    check_permutation(order, chunks)
-    # relative pace: the key (r + 1/2) / chunks never decreases along the order
-    keys = [(r + 0.5) / chunks[j] for j, r in order]
-    assert keys == sorted(keys)
-
-
-def test_windows_of_jobs_by_buffer_size(tmp_path):
-    # 40 jobs of 10 MB and 5 chunks each: windows of 16 jobs (160 MB > 64 MB,
-    # so the minimum count decides), i.e. jobs 0-15, 16-31, 32-39
-    chunks, mbs = [5] * 40, [10] * 40
-    out = run_order(tmp_path, chunks, mbs, True)
-    order = out["order"]
-    check_permutation(order, chunks)
-    assert out["min_jobs"] == 16 and out["window_mb"] == 64
-    windows = [j // 16 for j, _ in order]
-    assert windows == sorted(windows), "one window after another"
-    # small buffers: more jobs per window while they fit 64 MB (1 MB each)
-    out = run_order(tmp_path, [3] * 100, [1] * 100, True)
-    first = [j for j, _ in out["order"][:64 * 3]]
-    assert max(first) == 63 and min(first) == 0
-
-
-def test_windows_hold_min_chunks(tmp_path):
-    # 40 jobs of one chunk: with min_chunks 30 a window spans 30 jobs
-    out = run_order(tmp_path, [1] * 40, [10] * 40, True, min_chunks=30)
-    order = out["order"]
-    check_permutation(order, [1] * 40)
-    assert [j for j, _ in order[:30]] == list(range(30))
-    assert sorted(j for j, _ in order[30:]) == list(range(30, 40))
+def test_no_chunks_no_order(order_of):
+    assert order_of([0, 0]) == []
