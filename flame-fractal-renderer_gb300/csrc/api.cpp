@@ -1294,14 +1294,21 @@ ffr_status ffr_jit_prepare(const char* json, size_t len, const ffr_opts* opts)
     {
         return fail(nullptr, FFR_ERR_PARSE, e.what());
     }
-    for (const std::string& src : srcs)
-    {
-        if (src.empty())
-            continue;       // FP32 merged form, or no sorted kernel for the flame
-        std::string err;
-        if (!jit_compile_only(src, o.precision, &err))
-            return fail(nullptr, FFR_ERR_CUDA, err);
-    }
+    // the kernels compile in parallel (an empty source: FP32 merged form, or
+    // no sorted kernel for the flame)
+    std::vector<std::string> errs(srcs.size());
+    std::vector<char> ok(srcs.size(), 1);
+    std::vector<std::thread> threads;
+    for (size_t i = 0; i < srcs.size(); ++i)
+        if (!srcs[i].empty())
+            threads.emplace_back([&, i] {
+                ok[i] = jit_compile_only(srcs[i], o.precision, &errs[i]) ? 1 : 0;
+            });
+    for (std::thread& t : threads)
+        t.join();
+    for (size_t i = 0; i < srcs.size(); ++i)
+        if (!ok[i])
+            return fail(nullptr, FFR_ERR_CUDA, errs[i]);
     return FFR_OK;
 }
 

@@ -17,19 +17,31 @@ if [ ! -d "$REF_ROOT/src" ]; then
     exit 1
 fi
 mkdir -p "$HERE/_ref"
-g++ -std=c++23 -O3 -DNDEBUG -ffp-contract=off -w \
-    -I "$HERE/shim" -I "$HERE/shim/nest/nest" -I "$REF_ROOT/src" \
-    "$HERE/ref_driver.cpp" \
-    "$REF_ROOT/src/rng/flame_rng.cpp" \
-    "$REF_ROOT/src/utils/json.cpp" \
-    -o "$HERE/_ref/ffr_ref" -lpthread
+# rebuild a binary only when a source it is built from (the reference's
+# sources, the shims, the drivers, this script) is newer than it
+stale() {
+    local out="$1"
+    [ ! -e "$out" ] && return 0
+    [ -n "$(find "$REF_ROOT/src" "$HERE/shim" "$HERE/ref_driver.cpp" "$HERE/img_driver.cpp" \
+            "${BASH_SOURCE[0]}" -newer "$out" -print -quit)" ]
+}
+if stale "$HERE/_ref/ffr_ref"; then
+    g++ -std=c++23 -O3 -DNDEBUG -ffp-contract=off -w \
+        -I "$HERE/shim" -I "$HERE/shim/nest/nest" -I "$REF_ROOT/src" \
+        "$HERE/ref_driver.cpp" \
+        "$REF_ROOT/src/rng/flame_rng.cpp" \
+        "$REF_ROOT/src/utils/json.cpp" \
+        -o "$HERE/_ref/ffr_ref" -lpthread
+fi
 # the reference's own ffr-img (src/ffr_img.cpp, unmodified) with the
 # project's Boost.GIL / program_options shims and an unencoded image writer
 # (oracle/img_driver.cpp) in place of libpng
-exec g++ -std=c++23 -O2 -DNDEBUG -ffp-contract=off -w \
-    -I "$HERE/shim" -I "$HERE/shim/nest/nest" -I "$REF_ROOT/src" \
-    "$HERE/img_driver.cpp" \
-    "$REF_ROOT/src/ffr_img.cpp" \
-    "$REF_ROOT/src/rng/flame_rng.cpp" \
-    "$REF_ROOT/src/utils/json.cpp" \
-    -o "$HERE/_ref/ffr_img_ref" -lpthread
+if stale "$HERE/_ref/ffr_img_ref"; then
+    g++ -std=c++23 -O2 -DNDEBUG -ffp-contract=off -w \
+        -I "$HERE/shim" -I "$HERE/shim/nest/nest" -I "$REF_ROOT/src" \
+        "$HERE/img_driver.cpp" \
+        "$REF_ROOT/src/ffr_img.cpp" \
+        "$REF_ROOT/src/rng/flame_rng.cpp" \
+        "$REF_ROOT/src/utils/json.cpp" \
+        -o "$HERE/_ref/ffr_img_ref" -lpthread
+fi

@@ -90,3 +90,31 @@ def test_prepare_rejects_bad_input(ffr):
     raw = CASES["d1_group0"].encode()
     assert lib.ffr_jit_prepare(raw, len(raw), ctypes.byref(o)) == ffr.FFR_ERR_ARG
     assert lib.ffr_jit_prepare(None, 0, None) == ffr.FFR_ERR_ARG
+
+
+def test_generated_source_fixes_slot_and_xform_types(ffr, tmp_path, monkeypatch):
+    """The per-flame sources (read back from the FFR_JIT_CACHE key files)
+    narrow each variation slot to the types it holds over the xforms (plain
+    kernel) and write each xform out with its own types (sorted kernel)."""
+    monkeypatch.setenv("FFR_JIT_CACHE", str(tmp_path))
+    flame = {"dimensions": 2, "size": [32, 32], "bounds": [[-2, 2], [-2, 2]],
+             "xforms": [{"weight": 1.0, "variations": [{"name": "handkerchief", "weight": 0.5},
+                                                       {"name": "julia", "weight": 0.5}]},
+                        {"weight": 0.5, "variations": [{"name": "spherical", "weight": 0.5},
+                                                       {"name": "disc", "weight": 0.5}]}],
+             "final_xform": {"variations": [{"name": "linear", "weight": 1.0}]}}
+    assert ffr.jit_prepare(json.dumps(flame), ffr.FP32)[0] == ffr.FFR_OK
+    keys = [open(k).read() for k in glob.glob(str(tmp_path / "ffr_*.key"))]
+    plain = [k for k in keys if "ffr_flame_render(" in k]
+    sorted_ = [k for k in keys if "ffr_flame_sorted(" in k]
+    assert len(plain) == 1 and len(sorted_) == 1
+    # slot 0: handkerchief (id 24) and the benchmark types spherical and
+    # linear (kTa bits 4 | 1); slot 1: disc (id 26) and julia (bit 64)
+    assert "SlotTypes<D, R, 5u, 24>" in plain[0]
+    assert "SlotTypes<D, R, 64u, 26>" in plain[0]
+    assert "static constexpr int slots = 2;" in plain[0]
+    # xforms sorted by weight: xform 0 = handkerchief julia, xform 1 =
+    # spherical disc, then the final (linear); 2-D pre-affines absent
+    assert "FixedXform<D, R, 64u, false, false, 0, 24, 35>" in sorted_[0]
+    assert "FixedXform<D, R, 4u, false, false, 2, 2, 26>" in sorted_[0]
+    assert "FixedXform<D, R, 1u, false, false, 4, 0>" in sorted_[0]
