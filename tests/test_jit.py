@@ -118,3 +118,19 @@ def test_generated_source_fixes_slot_and_xform_types(ffr, tmp_path, monkeypatch)
     assert "FixedXform<D, R, 64u, false, false, 0, 24, 35>" in sorted_[0]
     assert "FixedXform<D, R, 4u, false, false, 2, 2, 26>" in sorted_[0]
     assert "FixedXform<D, R, 1u, false, false, 4, 0>" in sorted_[0]
+
+
+def test_sorted_kernel_only_where_the_sorted_kernel_runs(ffr, tmp_path, monkeypatch):
+    """Above 16 xforms the xform-sorted kernel does not run: preparing both
+    kernels compiles the plain one only, and asking for the sorted one
+    alone compiles nothing (renders then refuse FFR_KERNEL_JIT_SORTED)."""
+    monkeypatch.setenv("FFR_JIT_CACHE", str(tmp_path))
+    flame = {"dimensions": 2, "size": [16, 16], "bounds": [[-2, 2], [-2, 2]],
+             "xforms": [{"weight": 1.0 + k, "variations": [{"name": "heart", "weight": 1.0}]}
+                        for k in range(20)]}
+    text = json.dumps(flame)
+    assert ffr.jit_prepare(text, ffr.FP32, ffr.KERNEL_JIT_SORTED)[0] == ffr.FFR_OK
+    assert glob.glob(str(tmp_path / "ffr_*.key")) == []
+    assert ffr.jit_prepare(text, ffr.FP32)[0] == ffr.FFR_OK
+    keys = [open(k).read() for k in glob.glob(str(tmp_path / "ffr_*.key"))]
+    assert len(keys) == 1 and "ffr_flame_render(" in keys[0]
