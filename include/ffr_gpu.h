@@ -97,7 +97,8 @@ typedef struct ffr_opts {
    reference's XForm::applyIteration, src/types/xform.hpp:211-227,
    dispatches through virtual calls), compiled on the first render that
    needs it unless ffr_jit_prepare compiled it, cached per process and, with
-   FFR_JIT_CACHE naming a directory, on disk; FP32 programs of the seven
+   FFR_JIT_CACHE naming a directory (writable by this user alone: its cubins
+   are loaded and run), on disk; FP32 programs of the seven
    benchmark variations run their precompiled merged instantiation instead
    (stats.kernel PLAIN).  JIT_SORTED: the xform-sorted kernel compiled the
    same way, its warps running each xform's own code (flames of 1..3 dims and
