@@ -957,8 +957,8 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
     double* pcol = r ? reinterpret_cast<double*>(buf + off_col) : nullptr;
     DevStats* pst = reinterpret_cast<DevStats*>(buf + off_st);
     unsigned long long* phs = reinterpret_cast<unsigned long long*>(buf + off_hs);
-    const uint64_t P = std::min<uint64_t>(samples, c->opts.precision == FFR_FP64 ? (1u << 22)
-                                                                                 : (1u << 24));
+    uint64_t P = std::min<uint64_t>(samples, c->opts.precision == FFR_FP64 ? (1u << 22)
+                                                                           : (1u << 24));
     float best = 1e30f;
     int best_k = *kernel, best_a = 0;
     bool best_h = false;
@@ -984,6 +984,9 @@ ffr_status autotune(ffr_ctx* c, uint64_t samples, int* kernel, int* agg, bool* h
         {
             const uint64_t ntraj = (samples + L0 - 1) / L0;
             probe_streams = std::max<uint64_t>(1, std::min<uint64_t>(S0, ntraj));
+            // a render on few streams: probes of about 2048 samples per
+            // stream (at least 2^20), not 2^24 samples on a few threads
+            P = std::min<uint64_t>(P, std::max<uint64_t>(1u << 20, probe_streams * 2048));
             probe_len = std::max<uint64_t>(1, P / probe_streams);
         }
     }
